@@ -1,0 +1,243 @@
+/*
+ * pp_gb300.h -- C ABI of the GB300-native bond-based peridynamics time step.
+ *
+ * Every entry point takes device pointers (allocated by the caller), sizes,
+ * scalars and a CUDA stream passed as `void*` (NULL = the legacy default
+ * stream).  Nothing here allocates device memory, synchronises the stream or
+ * throws; each call returns PP_SUCCESS or one of the PP_ERROR_* codes below,
+ * and pp_status_string() turns a code into text.  Launch errors are read
+ * with cudaGetLastError() right after the launch and returned as
+ * PP_ERROR_CUDA; asynchronous kernel faults surface at the caller's next
+ * synchronisation, as for any CUDA library.
+ *
+ * Array layouts follow PeriPy's device integrators (peripy/integrators.py
+ * :84-254): node arrays are row-major (nnodes, 3) float64 or int32, the
+ * neighbour list is (nnodes, max_neigh) int32 padded and broken with -1,
+ * max_neigh a power of two (peripy/model.py:575-578).
+ *
+ * Each declaration names the reference interface it replaces.
+ */
+#ifndef PP_GB300_H
+#define PP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PP_ABI_VERSION 1
+
+/* Status codes. */
+#define PP_SUCCESS                  0
+#define PP_ERROR_INVALID_VALUE      1  /* bad size, NULL pointer or flag   */
+#define PP_ERROR_MAX_NEIGH          2  /* max_neigh not a power of 2 <= 1024 */
+#define PP_ERROR_MISALIGNED         3  /* pointer not aligned as required  */
+#define PP_ERROR_UNSUPPORTED        4  /* option combination not built     */
+#define PP_ERROR_CUDA               5  /* a CUDA runtime call failed       */
+
+/* Integrator kinds (peripy/integrators.py:462, 544, 651). */
+#define PP_EULER                    0
+#define PP_EULER_CROMER             1
+#define PP_VELOCITY_VERLET          2
+
+/* Arithmetic of the fused step. */
+#define PP_FLOAT64                  0  /* IEEE binary64 throughout          */
+#define PP_MIXED                    1  /* FP32 bonds, exact FP64 stretch test,
+                                          double-float node state          */
+
+/* Flags of the fused step. */
+#define PP_FLAG_COMPENSATED         1  /* compensated (TwoSum) FP32 force sum */
+
+/* ------------------------------------------------------------------------ */
+/* Utility.                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Text for a status code (static storage). */
+const char* pp_status_string(int status);
+
+/* PP_ABI_VERSION of the loaded library. */
+int pp_abi_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Reference-structured FP64 kernels ("plain" step).                        */
+/* Same arithmetic, in the same operation order and with the same           */
+/* work-group tree reduction order, as PeriPy's OpenCL kernels; separate    */
+/* launches for bond force, displacement update and damage.                 */
+/* ------------------------------------------------------------------------ */
+
+typedef struct pp_bond_force_args {
+    int32_t nnodes;
+    int32_t max_neigh;             /* power of two, 1..1024               */
+    int32_t nregimes;              /* used when bond_types != NULL         */
+    int32_t nbond_types;           /* used when bond_types != NULL         */
+    const double* u;               /* (nnodes,3)                           */
+    double* force;                 /* (nnodes,3) out                       */
+    double* body_force;            /* (nnodes,3) out                       */
+    const double* r0;              /* (nnodes,3)                           */
+    const double* vols;            /* (nnodes)                             */
+    int32_t* nlist;                /* (nnodes,max_neigh) in/out, -1 broken */
+    const int32_t* fc_types;       /* (nnodes,3)                           */
+    const double* fc_values;       /* (nnodes,3)                           */
+    const double* stiffness_corrections; /* (nnodes,max_neigh) or NULL     */
+    const int32_t* bond_types;     /* (nnodes,max_neigh) or NULL           */
+    int32_t* regimes;              /* (nnodes,max_neigh) in/out; with bond_types */
+    const double* plus_cs;         /* (nbond_types*nregimes); with bond_types */
+    const double* bond_stiffness_table;   /* (nbond_types*nregimes); with bond_types */
+    const double* critical_stretch_table; /* (nbond_types*nregimes); with bond_types */
+    double bond_stiffness;         /* scalar; without bond_types           */
+    double critical_stretch;       /* scalar; without bond_types           */
+    double fc_scale;               /* force_bc_magnitude of this step      */
+} pp_bond_force_args;
+
+/* Replaces bond_force1..bond_force4 (peripy/cl/peridynamics.cl:4-565),
+ * selected as peripy/integrators.py:109-148 does: by whether
+ * stiffness_corrections and bond_types are NULL. */
+int pp_bond_force(const pp_bond_force_args* args, void* stream);
+
+/* Replaces damage (peripy/cl/peridynamics.cl:568-610):
+ * n_neigh[i] = intact slots of row i, damage[i] = 1 - n_neigh[i]/family[i]. */
+int pp_damage(const int32_t* nlist, const int32_t* family, int32_t* n_neigh,
+              double* damage, int32_t nnodes, int32_t max_neigh,
+              void* stream);
+
+/* Replaces update_displacement of peripy/cl/euler.cl:3-24 (one DOF per
+ * element, ndof = 3*nnodes). */
+int pp_update_displacement_euler(const double* force, double* u,
+                                 const int32_t* bc_types,
+                                 const double* bc_values, double bc_scale,
+                                 double dt, int64_t ndof, void* stream);
+
+/* Replaces update_displacement of peripy/cl/euler_cromer.cl:3-35. */
+int pp_update_displacement_euler_cromer(
+    const double* force, double* u, double* ud, double* udd,
+    const int32_t* bc_types, const double* bc_values,
+    const double* densities, double bc_scale, double damping, double dt,
+    int64_t ndof, void* stream);
+
+/* Replaces update_displacement of peripy/cl/velocity_verlet.cl:3-36. */
+int pp_update_displacement_velocity_verlet(
+    const double* force, double* u, double* ud, double* udd,
+    const int32_t* bc_types, const double* bc_values,
+    const double* densities, double bc_scale, double damping, double dt,
+    int64_t ndof, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Fused step: one launch per time step does stretch, break (n-linear       */
+/* regimes), force, per-node reduction, force boundary conditions, intact   */
+/* count and the integrator update.  Replaces the launch pair of            */
+/* EulerCL/EulerCromerCL/VelocityVerletCL.__call__                          */
+/* (peripy/integrators.py:484-503, 586-606, 700-720).                       */
+/*                                                                          */
+/* Displacements are double-buffered: a step reads state slot `parity` and  */
+/* writes slot `parity ^ 1`, so no node reads a displacement another node   */
+/* has already advanced.                                                    */
+/*                                                                          */
+/* PP_FLOAT64 keeps the reference layouts: u[2] (nnodes,3) f64, ud, udd,    */
+/* force, body_force (nnodes,3) f64, n_neigh and damage per node.  Bond     */
+/* arithmetic is bit-identical to the plain kernels.                        */
+/*                                                                          */
+/* PP_MIXED uses the compact layouts produced by pp_mixed_pack():           */
+/*   pos_q   (nnodes) int4 {qx,qy,qz, float-bits of vol}: fixed-point       */
+/*           positions, r0 = origin + q * pos_scale (pos_scale a power of 2)*/
+/*   uhi[2]  (nnodes) float4 {ux,uy,uz, max|u|}: FP32 displacement (high   */
+/*           part of the double-float pair), gathered by neighbours         */
+/*   ulo[2]  (nnodes) float4: low parts of the double-float displacement    */
+/*   vel     (nnodes) float4 x2 {hi; lo}: double-float velocity (EC, VV)    */
+/*   acc     (nnodes) float4: FP32 acceleration (EC, VV)                    */
+/*   frc     (nnodes) float4 x2 {force; body_force} FP32                    */
+/*   rho32   (nnodes) float4 FP32 densities (EC, VV)                        */
+/*   sc32    (nnodes,max_neigh) float stiffness corrections or NULL         */
+/* and reads the reference r0 (f64) and the double-float displacement only  */
+/* for bonds whose FP32 stretch lies within a proven error band of a        */
+/* critical stretch; there the break/regime decision is taken from the      */
+/* binary64 stretch formula of peridynamics.cl:65-75, so it is the          */
+/* decision binary64 arithmetic makes on the same state.                    */
+/* pp_mixed_export() writes the reference-layout f64 arrays.                */
+/* ------------------------------------------------------------------------ */
+
+typedef struct pp_fused_args {
+    int32_t nnodes;
+    int32_t max_neigh;             /* power of two, 1..1024               */
+    int32_t integrator;            /* PP_EULER / PP_EULER_CROMER / PP_VELOCITY_VERLET */
+    int32_t precision;             /* PP_FLOAT64 / PP_MIXED                */
+    int32_t nregimes;
+    int32_t nbond_types;
+    int32_t flags;
+    int32_t nodes_per_block;       /* warps per block; 0 = default (8)     */
+    double dt;
+    double damping;
+    double bond_stiffness;         /* scalar when bond_types == NULL       */
+    double critical_stretch;       /* scalar when bond_types == NULL       */
+    const double* bond_stiffness_table;   /* with bond_types               */
+    const double* critical_stretch_table; /* with bond_types               */
+    const double* plus_cs;                /* with bond_types               */
+    /* static inputs, reference layouts */
+    const double* r0;
+    const double* vols;
+    const int32_t* family;
+    const int32_t* bc_types;
+    const double* bc_values;
+    const int32_t* fc_types;
+    const double* fc_values;
+    const double* densities;       /* EC / VV                              */
+    const double* stiffness_corrections;  /* or NULL                       */
+    const int32_t* bond_types;     /* or NULL                              */
+    /* mutable bond state */
+    int32_t* nlist;
+    int32_t* regimes;              /* with bond_types                      */
+    /* PP_FLOAT64 node state */
+    double* u[2];
+    double* ud;
+    double* udd;
+    double* force;
+    double* body_force;
+    int32_t* n_neigh;
+    double* damage;
+    /* PP_MIXED node state (16-byte aligned) */
+    int32_t* pos_q;
+    float* uhi[2];
+    float* ulo[2];
+    float* vel;                    /* 2*nnodes float4                      */
+    float* acc;
+    float* frc;                    /* 2*nnodes float4                      */
+    float* rho32;                  /* (nnodes) float4 densities (EC / VV)  */
+    float* sc32;
+    double pos_scale;
+    double pos_origin[3];
+} pp_fused_args;
+
+/* One fused step reading state slot `parity`; magnitudes of the
+ * displacement and force boundary conditions for this step by value. */
+int pp_fused_step(const pp_fused_args* args, int32_t parity,
+                  double displacement_bc_magnitude,
+                  double force_bc_magnitude, void* stream);
+
+/* `nsteps` fused steps starting at state slot `parity`, magnitudes read on
+ * the device from disp_mags[first + k] and force_mags[first + k]
+ * (k = 0..nsteps-1).  With use_graph != 0 the steps are captured in chunks
+ * of `chunk` (even) launches into one CUDA graph and replayed; the step
+ * index then comes from the device word *step_base (caller-allocated
+ * scratch, overwritten).  The final state is in slot parity ^ (nsteps & 1). */
+int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t nsteps,
+                 const double* disp_mags, const double* force_mags,
+                 int64_t first, int32_t use_graph, int32_t chunk,
+                 int64_t* step_base, void* stream);
+
+/* Builds the PP_MIXED layouts from the reference layouts: pos_q from r0 and
+ * vols (with args->pos_scale/pos_origin, which the caller chooses), the
+ * double-float displacement slot `parity` and velocity from u[parity] and
+ * ud, acc from udd, sc32 from stiffness_corrections.  Called by
+ * create_buffers (peripy/integrators.py:190-254). */
+int pp_mixed_pack(const pp_fused_args* args, int32_t parity, void* stream);
+
+/* Writes the reference layouts u[parity], ud, udd, force, body_force
+ * (float64) from the PP_MIXED state slot `parity`.  Called by write()
+ * (peripy/integrators.py:285-300). */
+int pp_mixed_export(const pp_fused_args* args, int32_t parity, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PP_GB300_H */

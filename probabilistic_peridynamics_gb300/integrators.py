@@ -1,0 +1,606 @@
+"""Integrators: the drop-in boundary of the time step.
+
+Mirrors PeriPy's ``Integrator`` API (``peripy/integrators.py:11-300``):
+``build`` (called once by ``Model.__init__``), ``create_buffers`` (called at
+the start of every ``Model.simulate``), ``__call__`` (one time step) and
+``write`` (device to host), with the same argument names, order, meaning
+and ``ValueError`` checks.  The OpenCL integrators ``EulerCL``,
+``EulerCromerCL`` and ``VelocityVerletCL`` (``integrators.py:462-764``) are
+replaced by :class:`EulerCUDA`, :class:`EulerCromerCUDA` and
+:class:`VelocityVerletCUDA`, which run hand-written sm_103a kernels through
+the C ABI of ``include/pp_gb300.h``; the old names are kept as aliases so a
+script only changes its import line.
+
+Each CUDA integrator takes two extra keyword arguments:
+
+``fused`` (default True)
+    True: one fused kernel per step (stretch, break, force, reduction,
+    boundary conditions, intact count, update).  False: the
+    reference-structured "plain" sequence of separate bond-force and update
+    kernels (``peripy/integrators.py:266-283, 530-541``).
+``precision`` (default ``"float64"``)
+    ``"float64"``: binary64 throughout, bit-identical to the reference
+    arithmetic.  ``"mixed"``: FP32 bond arithmetic, the break/regime test
+    decided exactly as binary64 would on the same state, and double-float
+    node state (fused only).
+
+Device memory is owned by the integrator as torch tensors; all work is
+queued on the context's CUDA stream and is asynchronous until ``write``.
+"""
+from abc import ABC, abstractmethod
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+
+
+class ContextError(Exception):
+    """No suitable CUDA device was found by :func:`get_context`."""
+
+    def __init__(self):
+        """Exception constructor (``peripy/integrators.py:767-775``)."""
+        message = ("No suitable context was found. You can manually specify "
+                   "the context by passing a CUDAContext to the integrator "
+                   "with the 'context' argument.")
+        super().__init__(message)
+
+
+class CUDAContext:
+    """A CUDA device and the stream all of an integrator's work runs on.
+
+    Replaces the pyopencl context and in-order queue the reference creates
+    in ``Integrator.__init__`` (``peripy/integrators.py:38-58``).  It is
+    truthy, which is what makes ``Model`` choose the power-of-two, ``-1``
+    padded neighbour-list layout (``peripy/model.py:575-585``).
+    """
+
+    def __init__(self, device=0, stream=None):
+        import torch
+        if not torch.cuda.is_available():
+            raise ContextError()
+        self.device = torch.device("cuda", device)
+        self.stream = (stream if stream is not None
+                       else torch.cuda.current_stream(self.device))
+
+    @property
+    def stream_handle(self):
+        return ctypes.c_void_p(self.stream.cuda_stream)
+
+    def __bool__(self):
+        return True
+
+    def __repr__(self):
+        return f"CUDAContext({self.device})"
+
+
+def get_context():
+    """Return a :class:`CUDAContext` on device 0, or None without a GPU.
+
+    Counterpart of ``peripy/cl/utilities.py:28-44``.
+    """
+    try:
+        import torch
+    except ImportError:  # pragma: no cover - torch is a hard dependency
+        return None
+    if not torch.cuda.is_available():
+        return None
+    return CUDAContext(0)
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _pos_frame(coords):
+    """Origin and power-of-two step of the fixed-point positions.
+
+    Positions become int32 ``q = (r0 - origin) / step`` with
+    ``|q| <= 2**29``, so neighbour differences are exact integers.
+    """
+    lo = coords.min(axis=0)
+    hi = coords.max(axis=0)
+    origin = (lo + hi) / 2
+    half = float(np.max(hi - lo) / 2)
+    if half <= 0.0:
+        half = 1.0
+    step = 2.0 ** (int(np.ceil(np.log2(half))) - 29)
+    return origin.astype(np.float64), step
+
+
+class Integrator(ABC):
+    """Base class for integrators (``peripy/integrators.py:11-300``).
+
+    Concrete integrators define ``__init__``, ``__call__``,
+    ``_build_special`` and ``_create_special_buffers``.
+    """
+
+    @abstractmethod
+    def __init__(self, dt, context=None):
+        """Create an :class:`Integrator` on a CUDA device.
+
+        :arg float dt: The length of time (in seconds [s]) of one time-step.
+        :arg context: Optional :class:`CUDAContext`; default is device 0.
+        :raises ContextError: when no CUDA device is available.
+        :raises TypeError: when ``context`` is not a :class:`CUDAContext`.
+        """
+        self.dt = dt
+        if context is None:
+            self.context = get_context()
+            if not isinstance(self.context, CUDAContext):
+                raise ContextError()
+        else:
+            if not isinstance(context, CUDAContext):
+                raise TypeError("context must be a CUDAContext object")
+            self.context = context
+        lib()  # fail loudly now if the CUDA library is missing
+
+    @abstractmethod
+    def __call__(self):
+        """Conduct one iteration of the integrator."""
+
+    @abstractmethod
+    def _build_special(self):
+        """Build what is special to the chosen integrator."""
+
+    @abstractmethod
+    def _create_special_buffers(self):
+        """Create buffers that are special to the chosen integrator."""
+
+
+class _CUDAIntegrator(Integrator):
+    """Shared implementation of the CUDA integrators."""
+
+    _kind = None          # PP_EULER / PP_EULER_CROMER / PP_VELOCITY_VERLET
+    _dynamic = False      # needs densities, ud, udd
+
+    def __init__(self, dt, context=None, fused=True, precision="float64",
+                 compensated=False, nodes_per_block=0, use_graph=True):
+        super().__init__(dt, context)
+        if precision not in ("float64", "mixed"):
+            raise ValueError("precision must be 'float64' or 'mixed' "
+                             f"(got {precision!r})")
+        if precision == "mixed" and not fused:
+            raise ValueError("precision='mixed' is implemented by the fused "
+                             "kernel only; use fused=True")
+        self.fused = bool(fused)
+        self.precision = precision
+        self.compensated = bool(compensated)
+        self.nodes_per_block = int(nodes_per_block)
+        self.use_graph = bool(use_graph)
+        self.damping = 0.0
+        self._parity = 0
+        self._fargs = None
+
+    # -------------------------------------------------------------- helpers
+    def _dev(self, array, dtype):
+        import torch
+        t = torch.as_tensor(np.ascontiguousarray(array, dtype=dtype))
+        return t.to(self.context.device, non_blocking=False)
+
+    def _empty(self, shape, dtype):
+        import torch
+        return torch.empty(shape, dtype=dtype, device=self.context.device)
+
+    def _zeros(self, shape, dtype):
+        import torch
+        return torch.zeros(shape, dtype=dtype, device=self.context.device)
+
+    @property
+    def _stream(self):
+        return self.context.stream_handle
+
+    # ---------------------------------------------------------------- build
+    def build(self, nnodes, degrees_freedom, max_neighbours, coords, volume,
+              family, bc_types, bc_values, force_bc_types, force_bc_values,
+              stiffness_corrections, bond_types, densities):
+        """Copy the simulate-independent arrays to the device.
+
+        Same arguments as ``peripy/integrators.py:84-188``.
+        """
+        import torch
+        self.nnodes = int(nnodes)
+        self.degrees_freedom = int(degrees_freedom)
+        self.max_neighbours = int(max_neighbours)
+        self.densities = densities
+        mn = self.max_neighbours
+        if mn < 1 or mn > 1024 or (mn & (mn - 1)):
+            raise ValueError(
+                "max_neighbours must be a power of two in [1, 1024] for CUDA "
+                f"integrators (got {mn})")
+        if self.degrees_freedom != 3:
+            raise ValueError("degrees_freedom must be 3 "
+                             f"(got {self.degrees_freedom})")
+        self.coords = np.ascontiguousarray(coords, dtype=np.float64)
+        self.r0_d = self._dev(self.coords, np.float64)
+        self.vols_d = self._dev(volume, np.float64)
+        self.family_d = self._dev(family, np.int32)
+        self.bc_types_d = self._dev(bc_types, np.int32)
+        self.bc_values_d = self._dev(bc_values, np.float64)
+        self.force_bc_types_d = self._dev(force_bc_types, np.int32)
+        self.force_bc_values_d = self._dev(force_bc_values, np.float64)
+        self.stiffness_corrections_d = (
+            None if stiffness_corrections is None
+            else self._dev(stiffness_corrections, np.float64))
+        self.bond_types_d = (None if bond_types is None
+                             else self._dev(bond_types, np.int32))
+        if self.bond_types_d is not None and (
+                tuple(self.bond_types_d.shape) != (self.nnodes, mn)):
+            raise ValueError("bond_types shape must be (nnodes, "
+                             "max_neighbours)")
+        self._torch = torch
+        self._build_special()
+
+    def _check_densities(self):
+        if self._dynamic:
+            if self.densities is None:
+                raise ValueError(
+                    "densities must be supplied when using {} integrator "
+                    "(got {}). This integrator is dynamic and requires the "
+                    "density or is_density argument to be supplied to "
+                    ":class:Model, alternatively, use a static integrator, "
+                    "such as EulerCUDA.".format(type(self).__name__,
+                                                type(self.densities)))
+            self.densities_d = self._dev(self.densities, np.float64)
+        else:
+            if self.densities is not None:
+                raise ValueError(
+                    "densities are not supported by this integrator "
+                    "(expected {}, got {}). This integrator neglects "
+                    "inertial effects. Do not supply a density or is_density "
+                    "argument or, alternatively, use a dynamic integrator, "
+                    "such as EulerCromerCUDA.".format(type(None),
+                                                      type(self.densities)))
+            self.densities_d = None
+
+    def _build_special(self):
+        """Check and upload the densities (``integrators.py:505-524``)."""
+        self._check_densities()
+
+    def _create_special_buffers(self):
+        """There are no integrator-specific buffers."""
+
+    # ------------------------------------------------------- create_buffers
+    def create_buffers(self, nlist, n_neigh, bond_stiffness,
+                       critical_stretch, plus_cs, u, ud, udd, force,
+                       body_force, damage, regimes, nregimes, nbond_types):
+        """Copy the simulate-dependent state to the device.
+
+        Same arguments as ``peripy/integrators.py:190-254``: with one bond
+        type and one regime the stiffness and critical stretch are kept as
+        ``np.float64`` scalars, else as device tables.
+        """
+        n, mn = self.nnodes, self.max_neighbours
+        if (nbond_types == 1) and (nregimes == 1):
+            self.bond_stiffness_d = np.float64(bond_stiffness)
+            self.critical_stretch_d = np.float64(critical_stretch)
+            self.plus_cs_d = None
+            self.regimes_d = None
+        else:
+            self.bond_stiffness_d = self._dev(
+                np.asarray(bond_stiffness).ravel(), np.float64)
+            self.critical_stretch_d = self._dev(
+                np.asarray(critical_stretch).ravel(), np.float64)
+            self.plus_cs_d = self._dev(np.asarray(plus_cs).ravel(),
+                                       np.float64)
+            self.regimes_d = self._dev(
+                np.zeros((n, mn)) if regimes is None else regimes, np.int32)
+            if self.bond_types_d is None:
+                self.bond_types_d = self._zeros((n, mn), self._torch.int32)
+        self.nregimes = np.intc(nregimes)
+        self.nbond_types = np.intc(nbond_types)
+        if self.bond_types_d is not None and self.plus_cs_d is None:
+            # Bond types with a single regime and type: one-entry tables.
+            self.plus_cs_d = self._dev(np.zeros(1), np.float64)
+            self.bond_stiffness_tab_d = self._dev(
+                np.atleast_1d(np.float64(bond_stiffness)), np.float64)
+            self.critical_stretch_tab_d = self._dev(
+                np.atleast_1d(np.float64(critical_stretch)), np.float64)
+            self.regimes_d = self._dev(
+                np.zeros((n, mn)) if regimes is None else regimes, np.int32)
+        elif self.plus_cs_d is not None:
+            self.bond_stiffness_tab_d = self.bond_stiffness_d
+            self.critical_stretch_tab_d = self.critical_stretch_d
+        else:
+            self.bond_stiffness_tab_d = None
+            self.critical_stretch_tab_d = None
+
+        torch = self._torch
+        self.nlist_d = self._dev(nlist, np.int32)
+        if tuple(self.nlist_d.shape) != (n, mn):
+            raise ValueError("nlist shape must be (nnodes, max_neighbours) = "
+                             f"{(n, mn)}, got {tuple(self.nlist_d.shape)}")
+        self.n_neigh_d = self._dev(n_neigh, np.int32)
+        self.u_d = [self._dev(u, np.float64).reshape(n, 3),
+                    self._empty((n, 3), torch.float64)]
+        self.ud_d = self._dev(ud, np.float64).reshape(n, 3)
+        self.udd_d = self._dev(udd, np.float64).reshape(n, 3)
+        self.force_d = self._zeros((n, 3), torch.float64)
+        self.body_force_d = self._zeros((n, 3), torch.float64)
+        self.damage_d = self._zeros((n,), torch.float64)
+        self._parity = 0
+        if self.precision == "mixed":
+            self._create_mixed_buffers()
+        self._fargs = self._make_fused_args() if self.fused else None
+        if self.precision == "mixed":
+            check(lib().pp_mixed_pack(ctypes.byref(self._fargs), 0,
+                                      self._stream), "pp_mixed_pack")
+        self._create_special_buffers()
+
+    def _create_mixed_buffers(self):
+        torch = self._torch
+        n, mn = self.nnodes, self.max_neighbours
+        self.pos_q_d = self._empty((n, 4), torch.int32)
+        self.uhi_d = [self._zeros((n, 4), torch.float32) for _ in range(2)]
+        self.ulo_d = [self._zeros((n, 4), torch.float32) for _ in range(2)]
+        self.frc_d = self._zeros((n, 8), torch.float32)
+        if self._dynamic:
+            self.vel_d = self._zeros((n, 8), torch.float32)
+            self.acc_d = self._zeros((n, 4), torch.float32)
+            self.rho32_d = self._zeros((n, 4), torch.float32)
+        else:
+            self.vel_d = self.acc_d = self.rho32_d = None
+        self.sc32_d = (None if self.stiffness_corrections_d is None
+                       else self._empty((n, mn), torch.float32))
+        self.pos_origin, self.pos_scale = _pos_frame(self.coords)
+
+    def _make_fused_args(self):
+        a = _lib.FusedArgs()
+        a.nnodes = self.nnodes
+        a.max_neigh = self.max_neighbours
+        a.integrator = self._kind
+        a.precision = (_lib.PP_MIXED if self.precision == "mixed"
+                       else _lib.PP_FLOAT64)
+        a.nregimes = int(self.nregimes)
+        a.nbond_types = int(self.nbond_types)
+        a.flags = _lib.PP_FLAG_COMPENSATED if self.compensated else 0
+        a.nodes_per_block = self.nodes_per_block
+        a.dt = float(self.dt)
+        a.damping = float(self.damping)
+        if isinstance(self.bond_stiffness_d, np.float64):
+            a.bond_stiffness = float(self.bond_stiffness_d)
+            a.critical_stretch = float(self.critical_stretch_d)
+        a.bond_stiffness_table = _ptr(self.bond_stiffness_tab_d)
+        a.critical_stretch_table = _ptr(self.critical_stretch_tab_d)
+        a.plus_cs = _ptr(self.plus_cs_d)
+        a.r0 = _ptr(self.r0_d)
+        a.vols = _ptr(self.vols_d)
+        a.family = _ptr(self.family_d)
+        a.bc_types = _ptr(self.bc_types_d)
+        a.bc_values = _ptr(self.bc_values_d)
+        a.fc_types = _ptr(self.force_bc_types_d)
+        a.fc_values = _ptr(self.force_bc_values_d)
+        a.densities = _ptr(self.densities_d)
+        a.stiffness_corrections = _ptr(self.stiffness_corrections_d)
+        a.bond_types = _ptr(self.bond_types_d)
+        a.nlist = _ptr(self.nlist_d)
+        a.regimes = _ptr(self.regimes_d)
+        a.u[0] = self.u_d[0].data_ptr()
+        a.u[1] = self.u_d[1].data_ptr()
+        a.ud = _ptr(self.ud_d)
+        a.udd = _ptr(self.udd_d)
+        a.force = _ptr(self.force_d)
+        a.body_force = _ptr(self.body_force_d)
+        a.n_neigh = _ptr(self.n_neigh_d)
+        a.damage = _ptr(self.damage_d)
+        if self.precision == "mixed":
+            a.pos_q = _ptr(self.pos_q_d)
+            a.uhi[0] = self.uhi_d[0].data_ptr()
+            a.uhi[1] = self.uhi_d[1].data_ptr()
+            a.ulo[0] = self.ulo_d[0].data_ptr()
+            a.ulo[1] = self.ulo_d[1].data_ptr()
+            a.vel = _ptr(self.vel_d)
+            a.acc = _ptr(self.acc_d)
+            a.frc = _ptr(self.frc_d)
+            a.rho32 = _ptr(self.rho32_d)
+            a.sc32 = _ptr(self.sc32_d)
+            a.pos_scale = float(self.pos_scale)
+            for k in range(3):
+                a.pos_origin[k] = float(self.pos_origin[k])
+        return a
+
+    # ----------------------------------------------------------------- step
+    def __call__(self, displacement_bc_magnitude, force_bc_magnitude):
+        """Conduct one iteration of the integrator.
+
+        :arg float displacement_bc_magnitude: the magnitude applied to the
+             displacement boundary conditions for the current time-step.
+        :arg float force_bc_magnitude: the magnitude applied to the force
+            boundary conditions for the current time-step.
+        """
+        if self.fused:
+            check(lib().pp_fused_step(
+                ctypes.byref(self._fargs), self._parity,
+                float(displacement_bc_magnitude), float(force_bc_magnitude),
+                self._stream), "pp_fused_step")
+            self._parity ^= 1
+        else:
+            self._bond_force(force_bc_magnitude)
+            self._update_displacement(displacement_bc_magnitude)
+
+    def _run(self, displacement_bc_magnitudes, force_bc_magnitudes, first,
+             steps):
+        """Run ``steps`` steps with magnitudes ``mags[first .. first+steps)``.
+
+        Equivalent to ``steps`` calls of ``__call__``; the fused path queues
+        them from C (optionally as a replayed CUDA graph), so Python adds no
+        per-step overhead.
+        """
+        if steps <= 0:
+            return
+        if not self.fused:
+            for k in range(first, first + steps):
+                self(displacement_bc_magnitudes[k], force_bc_magnitudes[k])
+            return
+        dm = self._dev(np.asarray(displacement_bc_magnitudes)[
+            first:first + steps], np.float64)
+        fm = self._dev(np.asarray(force_bc_magnitudes)[
+            first:first + steps], np.float64)
+        if not hasattr(self, "_step_base_d"):
+            self._step_base_d = self._zeros((1,), self._torch.int64)
+        check(lib().pp_fused_run(
+            ctypes.byref(self._fargs), self._parity, steps, _ptr(dm),
+            _ptr(fm), 0, int(self.use_graph), 16, _ptr(self._step_base_d),
+            self._stream), "pp_fused_run")
+        self._parity ^= steps & 1
+        # keep the magnitude arrays alive until the queued work has run
+        self._pending = (dm, fm)
+
+    def _bond_force(self, force_bc_magnitude):
+        """Plain bond-force launch (``integrators.py:266-283``)."""
+        a = _lib.BondForceArgs()
+        a.nnodes = self.nnodes
+        a.max_neigh = self.max_neighbours
+        a.nregimes = int(self.nregimes)
+        a.nbond_types = int(self.nbond_types)
+        a.u = _ptr(self.u_d[0])
+        a.force = _ptr(self.force_d)
+        a.body_force = _ptr(self.body_force_d)
+        a.r0 = _ptr(self.r0_d)
+        a.vols = _ptr(self.vols_d)
+        a.nlist = _ptr(self.nlist_d)
+        a.fc_types = _ptr(self.force_bc_types_d)
+        a.fc_values = _ptr(self.force_bc_values_d)
+        a.stiffness_corrections = _ptr(self.stiffness_corrections_d)
+        a.bond_types = _ptr(self.bond_types_d)
+        a.regimes = _ptr(self.regimes_d)
+        a.plus_cs = _ptr(self.plus_cs_d)
+        a.bond_stiffness_table = _ptr(self.bond_stiffness_tab_d)
+        a.critical_stretch_table = _ptr(self.critical_stretch_tab_d)
+        if isinstance(self.bond_stiffness_d, np.float64):
+            a.bond_stiffness = float(self.bond_stiffness_d)
+            a.critical_stretch = float(self.critical_stretch_d)
+        a.fc_scale = float(force_bc_magnitude)
+        check(lib().pp_bond_force(ctypes.byref(a), self._stream),
+              "pp_bond_force")
+
+    def _update_displacement(self, displacement_bc_magnitude):
+        raise NotImplementedError
+
+    # ---------------------------------------------------------------- write
+    def _sync_state(self):
+        """Bring the current state to the reference layouts on the device."""
+        L = lib()
+        if self.precision == "mixed":
+            check(L.pp_mixed_export(ctypes.byref(self._fargs), self._parity,
+                                    self._stream), "pp_mixed_export")
+        check(L.pp_damage(_ptr(self.nlist_d), _ptr(self.family_d),
+                          _ptr(self.n_neigh_d), _ptr(self.damage_d),
+                          self.nnodes, self.max_neighbours, self._stream),
+              "pp_damage")
+
+    def write(self, u, ud, udd, force, body_force, damage, nlist, n_neigh):
+        """Copy the state variables from device memory to host memory.
+
+        Computes the damage first, then fills the given host arrays in place
+        and returns them (``peripy/integrators.py:285-300``).
+        """
+        self._sync_state()
+        self.context.stream.synchronize()
+        cur = self.u_d[self._parity]
+
+        def put(host, dev):
+            src = dev.cpu().numpy()
+            if host is None:
+                return src
+            flat = host.reshape(-1)
+            flat[:src.size] = src.reshape(-1)[:flat.size]
+            return host
+
+        u = put(u, cur)
+        ud = put(ud, self.ud_d)
+        udd = put(udd, self.udd_d)
+        force = put(force, self.force_d)
+        body_force = put(body_force, self.body_force_d)
+        damage = put(damage, self.damage_d)
+        nlist = put(nlist, self.nlist_d)
+        n_neigh = put(n_neigh, self.n_neigh_d)
+        return (u, ud, udd, force, body_force, damage, nlist, n_neigh)
+
+
+class EulerCUDA(_CUDAIntegrator):
+    r"""Euler integrator on CUDA (replaces ``EulerCL``, integrators.py:462).
+
+    .. math::
+        u(t + \delta t) = u(t) + \delta t f(t)
+    """
+
+    _kind = _lib.PP_EULER
+    _dynamic = False
+
+    def __init__(self, *args, **kwargs):
+        """Create an :class:`EulerCUDA` integrator object."""
+        super().__init__(*args, **kwargs)
+
+    def _update_displacement(self, displacement_bc_magnitude):
+        check(lib().pp_update_displacement_euler(
+            _ptr(self.force_d), _ptr(self.u_d[0]), _ptr(self.bc_types_d),
+            _ptr(self.bc_values_d), float(displacement_bc_magnitude),
+            float(self.dt), 3 * self.nnodes, self._stream),
+            "pp_update_displacement_euler")
+
+
+class EulerCromerCUDA(_CUDAIntegrator):
+    r"""Euler-Cromer integrator on CUDA (replaces ``EulerCromerCL``).
+
+    .. math::
+        \ddot{u}(t) = \frac{f(t) - \eta \dot{u}(t)}{\rho},\quad
+        \dot{u}(t + \delta t) = \dot{u}(t) + \delta t \ddot{u}(t),\quad
+        u(t + \delta t) = u(t) + \delta t \dot{u}(t + \delta t)
+    """
+
+    _kind = _lib.PP_EULER_CROMER
+    _dynamic = True
+
+    def __init__(self, damping, *args, **kwargs):
+        """Create an :class:`EulerCromerCUDA` integrator object.
+
+        :arg float damping: The dynamic relaxation damping constant with
+            units [kg/(m^3 s)]
+        """
+        super().__init__(*args, **kwargs)
+        self.damping = damping
+
+    def _update_displacement(self, displacement_bc_magnitude):
+        check(lib().pp_update_displacement_euler_cromer(
+            _ptr(self.force_d), _ptr(self.u_d[0]), _ptr(self.ud_d),
+            _ptr(self.udd_d), _ptr(self.bc_types_d), _ptr(self.bc_values_d),
+            _ptr(self.densities_d), float(displacement_bc_magnitude),
+            float(self.damping), float(self.dt), 3 * self.nnodes,
+            self._stream), "pp_update_displacement_euler_cromer")
+
+
+class VelocityVerletCUDA(_CUDAIntegrator):
+    r"""Velocity-Verlet integrator on CUDA (replaces ``VelocityVerletCL``).
+
+    Uses the reference's own update (``peripy/cl/velocity_verlet.cl:90-94``):
+    the displacement advances by ``dt * (ud + dt/2 * udd)`` with the new
+    full-step velocity ``ud`` and acceleration ``udd``.
+    """
+
+    _kind = _lib.PP_VELOCITY_VERLET
+    _dynamic = True
+
+    def __init__(self, damping, *args, **kwargs):
+        """Create a :class:`VelocityVerletCUDA` integrator object.
+
+        :arg float damping: The dynamic relaxation damping constant with
+            units [kg/(m^3 s)]
+        """
+        super().__init__(*args, **kwargs)
+        self.damping = damping
+
+    def _update_displacement(self, displacement_bc_magnitude):
+        check(lib().pp_update_displacement_velocity_verlet(
+            _ptr(self.force_d), _ptr(self.u_d[0]), _ptr(self.ud_d),
+            _ptr(self.udd_d), _ptr(self.bc_types_d), _ptr(self.bc_values_d),
+            _ptr(self.densities_d), float(displacement_bc_magnitude),
+            float(self.damping), float(self.dt), 3 * self.nnodes,
+            self._stream), "pp_update_displacement_velocity_verlet")
+
+
+# Drop-in names of the reference's device integrators.
+EulerCL = EulerCUDA
+EulerCromerCL = EulerCromerCUDA
+VelocityVerletCL = VelocityVerletCUDA

@@ -1,0 +1,117 @@
+"""C-ABI library checks that need no GPU.
+
+* ``libpp_gb300.so`` loads and exports every function ``include/pp_gb300.h``
+  declares, with the ctypes mirror structs sized like the C structs;
+* argument validation runs on the host, before any CUDA call, and returns
+  the documented status codes;
+* the fixed-point position frame is exact for neighbour differences.
+"""
+import ctypes
+import pathlib
+import re
+
+import numpy as np
+import pytest
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "pp_gb300.h"
+
+
+@pytest.fixture(scope="module")
+def L():
+    from probabilistic_peridynamics_gb300 import _lib
+    if not _lib.LIB_PATH.exists():
+        from probabilistic_peridynamics_gb300 import build
+        build.build()
+    return _lib.lib()
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pp_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_functions_exported(L):
+    from probabilistic_peridynamics_gb300 import _lib
+    names = declared_functions()
+    assert names, "no declarations parsed"
+    for name in names:
+        assert hasattr(L, name), f"{name} not exported"
+    assert set(names) == set(_lib.SIGNATURES), (
+        "ctypes signatures out of sync with the header")
+
+
+def test_abi_version_and_status_strings(L):
+    assert L.pp_abi_version() == 1
+    assert L.pp_status_string(0) == b"success"
+    assert b"power of two" in L.pp_status_string(2)
+
+
+def test_struct_layout_matches_header():
+    """Field order and sizes of the ctypes mirrors (LP64 C layout)."""
+    from probabilistic_peridynamics_gb300 import _lib
+    # pp_bond_force_args: 4 int32, 14 pointers, 3 doubles
+    assert ctypes.sizeof(_lib.BondForceArgs) == 4 * 4 + 14 * 8 + 3 * 8
+    # pp_fused_args: 8 int32, 4 doubles, 45-8=... counted field by field
+    f = dict((n, getattr(_lib.FusedArgs, n)) for n, _ in
+             _lib.FusedArgs._fields_)
+    assert f["dt"].offset == 32
+    assert f["bond_stiffness_table"].offset == 64
+    assert f["pos_origin"].offset + 24 == ctypes.sizeof(_lib.FusedArgs)
+
+
+def test_validation_without_gpu(L):
+    from probabilistic_peridynamics_gb300 import _lib
+    a = _lib.BondForceArgs()
+    a.nnodes, a.max_neigh = 10, 3
+    assert L.pp_bond_force(ctypes.byref(a), None) == _lib.PP_ERROR_MAX_NEIGH
+    a.max_neigh = 2048
+    assert L.pp_bond_force(ctypes.byref(a), None) == _lib.PP_ERROR_MAX_NEIGH
+    a.max_neigh = 4
+    # NULL pointers with nnodes > 0
+    assert L.pp_bond_force(ctypes.byref(a), None) == \
+        _lib.PP_ERROR_INVALID_VALUE
+    assert L.pp_bond_force(None, None) == _lib.PP_ERROR_INVALID_VALUE
+    a.nnodes = 0
+    assert L.pp_bond_force(ctypes.byref(a), None) == _lib.PP_SUCCESS
+    assert L.pp_damage(None, None, None, None, 5, 6, None) == \
+        _lib.PP_ERROR_MAX_NEIGH
+    assert L.pp_update_displacement_euler(None, None, None, None, 0.0, 1.0,
+                                          -1, None) == \
+        _lib.PP_ERROR_INVALID_VALUE
+    fa = _lib.FusedArgs()
+    fa.nnodes, fa.max_neigh = 4, 4
+    assert L.pp_fused_step(ctypes.byref(fa), 2, 0.0, 0.0, None) == \
+        _lib.PP_ERROR_INVALID_VALUE
+    fa.integrator = 7
+    assert L.pp_fused_step(ctypes.byref(fa), 0, 0.0, 0.0, None) == \
+        _lib.PP_ERROR_INVALID_VALUE
+    fa.integrator = 0
+    fa.precision = 9
+    assert L.pp_fused_step(ctypes.byref(fa), 0, 0.0, 0.0, None) == \
+        _lib.PP_ERROR_INVALID_VALUE
+    # misaligned mixed-precision pointers are rejected before any launch
+    buf = (ctypes.c_char * 64)()
+    base = ctypes.addressof(buf)
+    for name in ("r0", "vols", "family", "bc_types", "bc_values",
+                 "fc_types", "fc_values", "nlist", "n_neigh", "frc"):
+        setattr(fa, name, base)
+    fa.precision = _lib.PP_MIXED
+    fa.pos_q = base + 4
+    fa.uhi[0] = fa.uhi[1] = fa.ulo[0] = fa.ulo[1] = base
+    fa.pos_scale = 1.0
+    assert L.pp_fused_step(ctypes.byref(fa), 0, 0.0, 0.0, None) == \
+        _lib.PP_ERROR_MISALIGNED
+
+
+def test_fixed_point_frame_exact_differences():
+    from probabilistic_peridynamics_gb300.integrators import _pos_frame
+    rng = np.random.default_rng(0)
+    coords = rng.uniform(-3.0, 5.0, size=(1000, 3))
+    origin, step = _pos_frame(coords)
+    assert np.log2(step) == int(np.log2(step))  # a power of two
+    q = np.rint((coords - origin) / step)
+    assert np.all(np.abs(q) <= 2 ** 29)
+    # reconstruction error below one step, differences exact integers
+    assert np.all(np.abs(origin + q * step - coords) <= step / 2)
