@@ -61,8 +61,15 @@ class CUDAContext:
         if not torch.cuda.is_available():
             raise ContextError()
         self.device = torch.device("cuda", device)
+        # A dedicated (capturable) stream unless the caller gives one; all
+        # of an integrator's torch copies and kernels are ordered on it.
         self.stream = (stream if stream is not None
-                       else torch.cuda.current_stream(self.device))
+                       else torch.cuda.Stream(self.device))
+
+    def on_stream(self):
+        """Context manager that makes this stream torch's current one."""
+        import torch
+        return torch.cuda.stream(self.stream)
 
     @property
     def stream_handle(self):
@@ -199,6 +206,15 @@ class _CUDAIntegrator(Integrator):
 
         Same arguments as ``peripy/integrators.py:84-188``.
         """
+        with self.context.on_stream():
+            self._build(nnodes, degrees_freedom, max_neighbours, coords,
+                        volume, family, bc_types, bc_values, force_bc_types,
+                        force_bc_values, stiffness_corrections, bond_types,
+                        densities)
+
+    def _build(self, nnodes, degrees_freedom, max_neighbours, coords, volume,
+               family, bc_types, bc_values, force_bc_types, force_bc_values,
+               stiffness_corrections, bond_types, densities):
         import torch
         self.nnodes = int(nnodes)
         self.degrees_freedom = int(degrees_freedom)
@@ -271,6 +287,14 @@ class _CUDAIntegrator(Integrator):
         type and one regime the stiffness and critical stretch are kept as
         ``np.float64`` scalars, else as device tables.
         """
+        with self.context.on_stream():
+            self._create_buffers(nlist, n_neigh, bond_stiffness,
+                                 critical_stretch, plus_cs, u, ud, udd,
+                                 regimes, nregimes, nbond_types)
+
+    def _create_buffers(self, nlist, n_neigh, bond_stiffness,
+                        critical_stretch, plus_cs, u, ud, udd, regimes,
+                        nregimes, nbond_types):
         n, mn = self.nnodes, self.max_neighbours
         if (nbond_types == 1) and (nregimes == 1):
             self.bond_stiffness_d = np.float64(bond_stiffness)
@@ -433,6 +457,12 @@ class _CUDAIntegrator(Integrator):
             for k in range(first, first + steps):
                 self(displacement_bc_magnitudes[k], force_bc_magnitudes[k])
             return
+        with self.context.on_stream():
+            self._run_fused(displacement_bc_magnitudes, force_bc_magnitudes,
+                            first, steps)
+
+    def _run_fused(self, displacement_bc_magnitudes, force_bc_magnitudes,
+                   first, steps):
         dm = self._dev(np.asarray(displacement_bc_magnitudes)[
             first:first + steps], np.float64)
         fm = self._dev(np.asarray(force_bc_magnitudes)[
@@ -496,6 +526,11 @@ class _CUDAIntegrator(Integrator):
         Computes the damage first, then fills the given host arrays in place
         and returns them (``peripy/integrators.py:285-300``).
         """
+        with self.context.on_stream():
+            return self._write(u, ud, udd, force, body_force, damage, nlist,
+                               n_neigh)
+
+    def _write(self, u, ud, udd, force, body_force, damage, nlist, n_neigh):
         self._sync_state()
         self.context.stream.synchronize()
         cur = self.u_d[self._parity]
