@@ -1,0 +1,575 @@
+#!/usr/bin/env python
+"""Headline benchmark: bond-updates/s of the fused mixed-precision step.
+
+Workload (the large plain-method configuration): a 200 x 200 x 10 regular
+lattice, dx = 0.005 (a 1 x 1 x 0.05 plate), horizon 3.015 dx, node volume
+dx^3, PMB bonds with c = 18 K / (pi delta^4), K = 1e9, s0 = 0.005; a
+pre-crack removes every bond crossing the plane x = 0.5 at y < 0.25; the
+x-min and x-max faces are pulled apart by 1e-8 per step; Velocity-Verlet
+with density 2400, damping 2.5e6 and dt = 1e-6.  400,000 nodes and
+42,700,528 directed bonds (one bond-update = one directed family bond in
+one step, counted on the initial connectivity).
+
+Arms
+----
+``python bench.py [--gpus N] [--steps K] [--warmup W]``
+    Our CUDA step.  ``value`` is the device-timed fused mixed-precision
+    (FP32 bonds, exact FP64 stretch test, double-float state) throughput
+    with the state resident in HBM; the plain and fused FP64 steps are timed
+    beside it (``variants``), the displacement error of the mixed step
+    against the FP64 step and the broken-bond mask are stated
+    (``accuracy``), ``e2e`` is a full 5000-step ``Model.simulate`` through
+    the public API with host arrays in and out, ``roofline`` relates the
+    fused kernel to the measured HBM bandwidth and ``cpu_baseline`` is the
+    reference's own CPU step timed on the host.
+``python bench.py --impl reference ...``
+    The reference's own CPU step (``peripy/peridynamics.pyx`` break_bonds +
+    bond_force + update_displacement, as ``Euler.__call__`` calls them),
+    compiled from its sources into ``oracle/_ref``, on a bounded slab of the
+    same lattice per step.
+
+Under torchrun every rank runs an independent replica on its own GPU (the
+configuration fits one GPU); ``value`` is the sum over ranks.
+"""
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = ("bond-updates/sec at 1 GB300, FP32 fused vs FP64 plain at stated "
+          "disp. error")
+UNIT = "bond-updates/s"
+WORKLOAD = ("pre-cracked 200x200x10 lattice, 400k nodes, 42.7M bonds, "
+            "Velocity-Verlet")
+NX, NY, NZ = 200, 200, 10
+DX = 0.005
+HORIZON_CELLS = 3.015
+BULK_MODULUS = 1e9
+S0 = 0.005
+DENSITY = 2400.0
+DAMPING = 2.5e6
+DT = 1e-6
+PULL_RATE = 1e-8
+E2E_STEPS = 5000
+#: reference-layout bytes per directed bond (int32 nlist read) and per node
+#: for Velocity-Verlet: reads u 24, r0 24, vol 8, bc_types 12, bc_values 24,
+#: force_bc_types 12, force_bc_values 24, family 4, ud 24, udd 24,
+#: densities 24; writes u 24, force 24, body_force 24, damage 8, n_neigh 4,
+#: ud 24, udd 24.
+B_BOND = 4
+B_NODE_VV = 336
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20000)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--fp64-steps", type=int, default=10,
+                   help="timed steps of each FP64 variant")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--accuracy-steps", type=int, default=E2E_STEPS)
+    p.add_argument("--profile", choices=["mixed", "fp64", "plain"],
+                   help="only run 3 warm-up and 3 profiled launches of one "
+                        "step variant on the full workload (for ncu)")
+    return p.parse_args()
+
+
+def profile_case(which):
+    """3 warm-up + 3 launches of one step variant, direct launches."""
+    import torch
+    w = build_workload()
+    precision = "mixed" if which == "mixed" else "float64"
+    integ = make_integrator(w, precision, which != "plain")
+    for k in range(6):
+        integ(PULL_RATE * (k + 1), 0.0)
+    integ.context.stream.synchronize()
+    torch.cuda.synchronize()
+    print(f"profile case {which}: 6 steps done", flush=True)
+
+
+# ----------------------------------------------------------------- workload
+def build_workload(pow2=True):
+    from probabilistic_peridynamics_gb300 import lattice
+    coords = lattice.lattice_coords(NX, NY, NZ, DX)
+    family, nlist, width = lattice.lattice_family(NX, NY, NZ, HORIZON_CELLS,
+                                                  pow2=pow2)
+    n_neigh = family.copy()
+    pairs = lattice.plane_crack_pairs(coords, nlist, n_neigh, 0.5, 0.25)
+    lattice.remove_pairs(pairs, nlist, n_neigh)
+    bc_types, bc_values = lattice.face_bcs(coords, 0)
+    n = coords.shape[0]
+    horizon = HORIZON_CELLS * DX
+    return dict(coords=coords, volume=np.full(n, DX ** 3), family=family,
+                nlist=nlist, n_neigh=n_neigh, bc_types=bc_types,
+                bc_values=bc_values,
+                force_bc_types=np.zeros((n, 3), dtype=np.intc),
+                force_bc_values=np.zeros((n, 3)),
+                densities=np.full((n, 3), DENSITY), nnodes=n,
+                max_neigh=int(width), horizon=horizon,
+                k=lattice.bond_stiffness_pmb(BULK_MODULUS, horizon), s0=S0,
+                bonds=int(family.sum()), crack_pairs=int(len(pairs)))
+
+
+def make_integrator(w, precision, fused, context=None):
+    import probabilistic_peridynamics_gb300 as pp
+    integ = pp.VelocityVerletCUDA(DAMPING, dt=DT, precision=precision,
+                                  fused=fused, context=context)
+    integ.build(w["nnodes"], 3, w["max_neigh"], w["coords"], w["volume"],
+                w["family"], w["bc_types"], w["bc_values"],
+                w["force_bc_types"], w["force_bc_values"], None, None,
+                w["densities"])
+    n = w["nnodes"]
+    z = np.zeros((n, 3))
+    integ.create_buffers(w["nlist"], w["n_neigh"], w["k"], w["s0"], None, z,
+                         z, z, z, z, np.zeros(n), None, 1, 1)
+    return integ
+
+
+# -------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}",
+                 f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
+                 "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap")
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                smax.append(float(parts[2].split()[0]))
+                power.append(float(parts[3].split()[0]))
+            except (ValueError, IndexError):
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        loaded = [s for s, p in zip(sm, power) if p > 300.0] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+# ------------------------------------------------------------ measurements
+def time_steps(integ, steps, warmup, torch, dist=None):
+    """Device time of exactly ``steps`` fused steps (graph replays)."""
+    dm = torch.as_tensor(PULL_RATE * np.arange(1, warmup + steps + 1),
+                         dtype=torch.float64, device=integ.context.device)
+    fm = torch.zeros_like(dm)
+    stream = integ.context.stream
+    if warmup:
+        integ._run_device(dm, fm, 0, warmup)
+    stream.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    integ._run_device(dm, fm, warmup, steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    return e0.elapsed_time(e1)
+
+
+def time_kernel_launches(integ, nlaunch, torch, first_mag=0.0):
+    """Mean duration of individual fused-step launches (events per launch)."""
+    stream = integ.context.stream
+    evs = [(torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True)) for _ in range(nlaunch)]
+    for k, (a, b) in enumerate(evs):
+        a.record(stream)
+        integ(first_mag + PULL_RATE * k, 0.0)
+        b.record(stream)
+    stream.synchronize()
+    return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+
+def time_plain_steps(integ, steps, warmup, torch):
+    stream = integ.context.stream
+    for k in range(warmup):
+        integ(PULL_RATE * (k + 1), 0.0)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(steps):
+        integ(PULL_RATE * (warmup + k + 1), 0.0)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def accuracy(w, steps, torch):
+    """Mixed vs FP64 fused (bit-identical to the plain FP64 step) after
+    ``steps`` steps from the same state: displacement error and mask."""
+    out = {}
+    for precision in ("float64", "mixed"):
+        integ = make_integrator(w, precision, True)
+        mags = PULL_RATE * np.arange(1, steps + 1)
+        integ._run(mags, np.zeros(steps), 0, steps)
+        n = w["nnodes"]
+        u, ud, udd, f, bf = (np.zeros((n, 3)) for _ in range(5))
+        res = integ.write(u, ud, udd, f, bf, np.zeros(n), w["nlist"].copy(),
+                          w["n_neigh"].copy())
+        out[precision] = res
+        del integ
+        torch.cuda.empty_cache()
+    u64, u32 = out["float64"][0], out["mixed"][0]
+    err = float(np.max(np.abs(u32 - u64)) / np.max(np.abs(u64)))
+    flips = int(np.sum(out["float64"][6] != out["mixed"][6]))
+    broken = int(np.sum(w["nlist"] != -1) - np.sum(out["float64"][6] != -1))
+    return {"steps": steps, "disp_rel_err_vs_fp64": err,
+            "mask_flips_vs_fp64": flips, "bonds_broken_fp64": broken,
+            "max_abs_u": float(np.max(np.abs(u64)))}
+
+
+def e2e_simulate(w, torch):
+    """Full 5000-step Model.simulate with host arrays in and out."""
+    import probabilistic_peridynamics_gb300 as pp
+    from probabilistic_peridynamics_gb300.mesh import write_vtk
+    tmp = tempfile.mkdtemp()
+    mesh = os.path.join(tmp, "lattice.vtk")
+    write_vtk(mesh, w["coords"], [])
+    lo, hi = w["coords"][:, 0].min(), w["coords"][:, 0].max()
+
+    def is_bnd(x):
+        if x[0] <= lo + 1e-9:
+            return [-1.0, None, None]
+        if x[0] >= hi - 1e-9:
+            return [1.0, None, None]
+        return [None, None, None]
+
+    integ = pp.VelocityVerletCUDA(DAMPING, dt=DT, precision="mixed")
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        model = pp.Model(mesh, integ, horizon=w["horizon"],
+                         critical_stretch=S0, bond_stiffness=w["k"],
+                         transfinite=1,
+                         volume_total=float(w["volume"].sum()),
+                         connectivity=(w["nlist"], w["n_neigh"]),
+                         family=w["family"], dimensions=3,
+                         density=np.full(w["nnodes"], DENSITY),
+                         is_displacement_boundary=is_bnd)
+    mags = PULL_RATE * np.arange(1, E2E_STEPS + 1)
+    model.simulate(steps=20, displacement_bc_magnitudes=mags)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u, damage, (nlist, n_neigh), force, ud, _ = model.simulate(
+        steps=E2E_STEPS, displacement_bc_magnitudes=mags)
+    torch.cuda.synchronize()
+    dt_s = time.perf_counter() - t0
+    n = w["nnodes"]
+    # create_buffers: nlist, n_neigh, u, ud, udd; per-segment magnitudes
+    h2d = (w["nlist"].nbytes + w["n_neigh"].nbytes + 3 * n * 24
+           + E2E_STEPS * 16)
+    d2h = 5 * n * 24 + n * 8 + nlist.nbytes + n_neigh.nbytes
+    return {"value": w["bonds"] * E2E_STEPS / dt_s, "unit": UNIT,
+            "h2d_bytes_per_step": h2d / E2E_STEPS,
+            "d2h_bytes_per_step": d2h / E2E_STEPS,
+            "steps": E2E_STEPS, "wall_s": dt_s,
+            "path": "Model.simulate (VelocityVerletCUDA, precision='mixed')"}
+
+
+# --------------------------------------------------------------- CPU side
+def reference_step_fn():
+    """The reference's CPU Euler step, or None when it is not built."""
+    try:
+        from oracle import build_ref
+        if not build_ref.available():
+            build_ref.build(quiet=True)
+        mod = build_ref.load()
+    except Exception:  # noqa: BLE001 - any failure means "not available"
+        return None
+    return mod
+
+
+def compact(nlist, family):
+    width = int(family.max())
+    out = np.ascontiguousarray(nlist[:, :width]).astype(np.intc)
+    out[out == -1] = 0
+    return out
+
+
+def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None):
+    """Time the reference CPU step on an nx x 200 x 10 slab of the lattice.
+
+    :returns: (bond-updates/s, steps run, seconds, bonds per step, kind,
+        cores)
+    """
+    from probabilistic_peridynamics_gb300 import lattice
+    coords = lattice.lattice_coords(nx, NY, NZ, DX)
+    family, nlist, _ = lattice.lattice_family(nx, NY, NZ, HORIZON_CELLS,
+                                              pow2=False)
+    n = coords.shape[0]
+    bonds = int(family.sum())
+    k = lattice.bond_stiffness_pmb(BULK_MODULUS, HORIZON_CELLS * DX)
+    bc_types, bc_values = lattice.face_bcs(coords, 0)
+    vol = np.full(n, DX ** 3)
+    fct = np.zeros((n, 3), dtype=np.intc)
+    fcv = np.zeros((n, 3))
+    u = np.zeros((n, 3))
+    n_neigh = family.copy()
+    mod = reference_step_fn()
+    if mod is not None:
+        nl = compact(nlist, family)
+
+        def step(s):
+            mod.break_bonds(coords + u, coords, nl, n_neigh, S0)
+            f = mod.bond_force(coords + u, coords, nl, n_neigh, vol, k, fcv,
+                               fct, 0.0)
+            mod.update_displacement(u, bc_values, bc_types, f,
+                                    PULL_RATE * s, DT)
+        kind, cores = "reference", 1
+    else:
+        from oracle import cref
+        st = cref.Stepper("euler", DT, coords, vol, family, nlist, bc_types,
+                          bc_values, fct, fcv, k, S0)
+
+        def step(s):
+            st.step(PULL_RATE * s, 0.0)
+        kind, cores = "port", os.cpu_count() or 1
+    t0 = time.perf_counter()
+    done = 0
+    while True:
+        step(done + 1)
+        done += 1
+        el = time.perf_counter() - t0
+        if steps is not None:
+            if done >= steps:
+                break
+        elif done >= max_steps or (el >= budget_s and done >= min_steps):
+            break
+    el = time.perf_counter() - t0
+    return bonds * done / el, done, el, bonds, kind, cores
+
+
+def cpu_baseline():
+    rate, steps, el, bonds, kind, cores = cpu_sample(NX, budget_s=10.0)
+    what = ("reference Cython Euler step (peripy/peridynamics.pyx break_bonds"
+            " + bond_force + update_displacement)" if kind == "reference"
+            else "C restatement of the OpenCL step (OpenMP)")
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"{steps} step(s) of the {what} on the full "
+                      f"{NX}x{NY}x{NZ} lattice ({bonds} bonds/step), "
+                      f"{el:.1f} s"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    total = args.steps + args.warmup
+    # Size the slab so that warm-up + timed steps take about 90 s.
+    probe_rate, *_ = cpu_sample(4, budget_s=0.5, min_steps=1, max_steps=3)
+    per_step_bonds = probe_rate * 90.0 / max(total, 1)
+    bonds_per_x = 42700528 / NX
+    nx = int(max(4, min(NX, per_step_bonds // bonds_per_x)))
+    from probabilistic_peridynamics_gb300 import lattice  # noqa: F401
+    if args.warmup:
+        cpu_sample(nx, 0.0, steps=args.warmup)
+    rate, steps, el, bonds, kind, cores = cpu_sample(nx, 0.0,
+                                                     steps=args.steps)
+    sample = (f"each step: the reference CPU step on a {nx}x{NY}x{NZ} slab "
+              f"of the lattice ({bonds} bonds)" if kind == "reference" else
+              f"each step: C restatement of the OpenCL step on a "
+              f"{nx}x{NY}x{NZ} slab ({bonds} bonds)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": sample,
+                   "integrator": "Euler (the reference CPU path has no "
+                                 "Velocity-Verlet)"},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores,
+                         "kind": kind, "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# -------------------------------------------------------------------- main
+def load_peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        return None
+
+
+def load_traffic():
+    """DRAM bytes per launch of the fused kernel from the committed ncu
+    summary (``profiles/*traffic*.txt``: a ``dram_bytes_per_launch N`` line)."""
+    for p in sorted((ROOT / "profiles").glob("*traffic*.txt")):
+        for line in p.read_text().splitlines():
+            if line.startswith("dram_bytes_per_launch"):
+                try:
+                    return float(line.split()[1])
+                except (IndexError, ValueError):
+                    pass
+    return None
+
+
+def main():
+    args = parse_args()
+    if args.profile:
+        profile_case(args.profile)
+        return
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    from probabilistic_peridynamics_gb300.integrators import CUDAContext
+    ctx = CUDAContext(local)
+    w = build_workload()
+    integ = make_integrator(w, "mixed", True, context=ctx)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = time_steps(integ, args.steps, args.warmup, torch, dist)
+    clk = clocks.stop()
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * w["bonds"] * args.steps / (ms * 1e-3)
+    kernel_ms = time_kernel_launches(integ, 200, torch)
+    launches = args.steps + (args.steps // 16 + 1
+                             if args.steps >= 32 else 0)
+    del integ
+    torch.cuda.empty_cache()
+    if rank != 0:
+        if dist is not None:
+            dist.barrier()
+        return
+
+    peaks = load_peaks()
+    peak = float(peaks["hbm_gbs"]) if peaks else 6800.0
+    alg_bytes = w["bonds"] * B_BOND + w["nnodes"] * B_NODE_VV
+    achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
+    traffic = load_traffic()
+
+    variants = {"fused_mixed": {"bond_updates_per_s": value,
+                                "ms_per_step": ms_per_step,
+                                "kernel_ms": kernel_ms}}
+    for name, precision, fused in (("plain_fp64", "float64", False),
+                                   ("fused_fp64", "float64", True)):
+        it = make_integrator(w, precision, fused, context=ctx)
+        if fused:
+            ms64 = time_steps(it, args.fp64_steps, 2, torch) / args.fp64_steps
+        else:
+            ms64 = time_plain_steps(it, args.fp64_steps, 2, torch)
+        variants[name] = {"bond_updates_per_s": w["bonds"] / (ms64 * 1e-3),
+                          "ms_per_step": ms64}
+        del it
+        torch.cuda.empty_cache()
+    variants["speedup_mixed_vs_plain_fp64"] = (
+        value / variants["plain_fp64"]["bond_updates_per_s"])
+
+    acc = accuracy(w, args.accuracy_steps, torch) if args.accuracy_steps \
+        else None
+    e2e = None if args.no_e2e else e2e_simulate(w, torch)
+    cpu = None if args.no_cpu else cpu_baseline()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nodes": w["nnodes"],
+                   "bonds": w["bonds"], "max_neigh": w["max_neigh"],
+                   "crack_pairs": w["crack_pairs"], "dt": DT,
+                   "integrator": "Velocity-Verlet", "density": DENSITY,
+                   "damping": DAMPING, "precision": "mixed (FP32 bonds, "
+                   "exact FP64 stretch test, double-float state)",
+                   "l2": "inputs larger than L2 (204.8 MB neighbour list "
+                         "streamed per step), no flush",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic,
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "kernel": "k_fused_mixed",
+                     "kernel_ms": kernel_ms,
+                     "peak_source": ("measured" if peaks else "fallback")},
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clk, "variants": variants, "accuracy": acc,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+
+
+if __name__ == "__main__":
+    main()

@@ -467,15 +467,21 @@ class _CUDAIntegrator(Integrator):
             first:first + steps], np.float64)
         fm = self._dev(np.asarray(force_bc_magnitudes)[
             first:first + steps], np.float64)
-        if not hasattr(self, "_step_base_d"):
-            self._step_base_d = self._zeros((1,), self._torch.int64)
-        check(lib().pp_fused_run(
-            ctypes.byref(self._fargs), self._parity, steps, _ptr(dm),
-            _ptr(fm), 0, int(self.use_graph), 16, _ptr(self._step_base_d),
-            self._stream), "pp_fused_run")
-        self._parity ^= steps & 1
+        self._run_device(dm, fm, 0, steps)
         # keep the magnitude arrays alive until the queued work has run
         self._pending = (dm, fm)
+
+    def _run_device(self, dm, fm, first, steps):
+        """Queue ``steps`` fused steps reading ``dm[first + k]`` and
+        ``fm[first + k]`` from device float64 tensors (no host copies)."""
+        if not hasattr(self, "_step_base_d"):
+            with self.context.on_stream():
+                self._step_base_d = self._zeros((1,), self._torch.int64)
+        check(lib().pp_fused_run(
+            ctypes.byref(self._fargs), self._parity, steps, _ptr(dm),
+            _ptr(fm), first, int(self.use_graph), 16,
+            _ptr(self._step_base_d), self._stream), "pp_fused_run")
+        self._parity ^= steps & 1
 
     def _bond_force(self, force_bc_magnitude):
         """Plain bond-force launch (``integrators.py:266-283``)."""
