@@ -138,8 +138,12 @@ int pp_update_displacement_velocity_verlet(
 /* arithmetic is bit-identical to the plain kernels.                        */
 /*                                                                          */
 /* PP_MIXED uses the compact layouts produced by pp_mixed_pack():           */
-/*   pos_q   (nnodes) int4 {qx,qy,qz, float-bits of vol}: fixed-point       */
-/*           positions, r0 = origin + q * pos_scale (pos_scale a power of 2)*/
+/*   pos_q   (nnodes) int4 {qx,qy,qz, w}: fixed-point positions,            */
+/*           r0 = origin + q * pos_scale, pos_scale a power of two with     */
+/*           pos_scale >= 2^-21 * pp_bond_extent() so that every bond's     */
+/*           |q[j] - q[i]| < 2^22 converts to float exactly without an      */
+/*           int-to-float instruction; w = float bits of k*vol (PMB) or of  */
+/*           vol (bond types)                                               */
 /*   uhi[2]  (nnodes) float4 {ux,uy,uz, max|u|}: FP32 displacement (high   */
 /*           part of the double-float pair), gathered by neighbours         */
 /*   ulo[2]  (nnodes) float4: low parts of the double-float displacement    */
@@ -147,6 +151,8 @@ int pp_update_displacement_velocity_verlet(
 /*   acc     (nnodes) float4: FP32 acceleration (EC, VV)                    */
 /*   frc     (nnodes) float4 x2 {force; body_force} FP32                    */
 /*   rho32   (nnodes) float4 FP32 densities (EC, VV)                        */
+/*   nflags  (nnodes) int: bit d set when bc_types[3i+d] != 0, bit 3+d when  */
+/*           fc_types[3i+d] != 0                                            */
 /*   sc32    (nnodes,max_neigh) float stiffness corrections or NULL         */
 /* and reads the reference r0 (f64) and the double-float displacement only  */
 /* for bonds whose FP32 stretch lies within a proven error band of a        */
@@ -203,6 +209,7 @@ typedef struct pp_fused_args {
     float* frc;                    /* 2*nnodes float4                      */
     float* rho32;                  /* (nnodes) float4 densities (EC / VV)  */
     float* sc32;
+    int32_t* nflags;               /* (nnodes) boundary-condition flags    */
     double pos_scale;
     double pos_origin[3];
 } pp_fused_args;
@@ -224,10 +231,17 @@ int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t nsteps,
                  int64_t first, int32_t use_graph, int32_t chunk,
                  int64_t* step_base, void* stream);
 
+/* Largest |r0[j][d] - r0[i][d]| over the bonds (i, j) of nlist (entries
+ * != -1) and the three components d, written to *extent (a caller-allocated
+ * device double).  The caller derives pos_scale for PP_MIXED from it. */
+int pp_bond_extent(const int32_t* nlist, const double* r0, int32_t nnodes,
+                   int32_t max_neigh, double* extent, void* stream);
+
 /* Builds the PP_MIXED layouts from the reference layouts: pos_q from r0 and
  * vols (with args->pos_scale/pos_origin, which the caller chooses), the
  * double-float displacement slot `parity` and velocity from u[parity] and
- * ud, acc from udd, sc32 from stiffness_corrections.  Called by
+ * ud, acc from udd, sc32 from stiffness_corrections, nflags from bc_types
+ * and fc_types.  Called by
  * create_buffers (peripy/integrators.py:190-254). */
 int pp_mixed_pack(const pp_fused_args* args, int32_t parity, void* stream);
 

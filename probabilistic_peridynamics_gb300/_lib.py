@@ -70,7 +70,7 @@ class FusedArgs(ctypes.Structure):
         ("body_force", _vp), ("n_neigh", _vp), ("damage", _vp),
         ("pos_q", _vp), ("uhi", _vp * 2), ("ulo", _vp * 2), ("vel", _vp),
         ("acc", _vp), ("frc", _vp), ("rho32", _vp), ("sc32", _vp),
-        ("pos_scale", _f64), ("pos_origin", _f64 * 3),
+        ("nflags", _vp), ("pos_scale", _f64), ("pos_origin", _f64 * 3),
     ]
 
 
@@ -94,6 +94,7 @@ SIGNATURES = {
         ctypes.c_int,
         [ctypes.POINTER(FusedArgs), _i32, _i64, _vp, _vp, _i64, _i32, _i32,
          _vp, _vp]),
+    "pp_bond_extent": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
     "pp_mixed_pack": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
     "pp_mixed_export": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
 }

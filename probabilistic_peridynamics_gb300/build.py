@@ -23,6 +23,10 @@ INCLUDE = HERE.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE)]
+#: Per-unit flags.  The mixed-precision step accepts flushed denormals and
+#: approximate FP32 division/square root: its error band covers them.
+UNIT_FLAGS = {"pp_mixed.cu": ["-ftz=true", "-prec-div=false",
+                              "-prec-sqrt=false"]}
 
 
 def _nvcc():
@@ -58,7 +62,8 @@ def build(force=False, verbose=False):
 
     def compile_one(job):
         src, obj = job
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *UNIT_FLAGS.get(src.name, []), "-c",
+               str(src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
         res = subprocess.run(cmd, capture_output=True, text=True)

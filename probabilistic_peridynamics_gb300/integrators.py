@@ -100,20 +100,24 @@ def _ptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
-def _pos_frame(coords):
+def _pos_frame(coords, extent):
     """Origin and power-of-two step of the fixed-point positions.
 
-    Positions become int32 ``q = (r0 - origin) / step`` with
-    ``|q| <= 2**29``, so neighbour differences are exact integers.
+    Positions become int32 ``q = rint((r0 - origin) / step)``.  The step is
+    the smallest power of two with ``extent / step <= 2**21``, where
+    ``extent`` is the largest bond component length, so every bond's
+    ``|q[j] - q[i]| < 2**22`` converts to float exactly; it is coarsened if
+    the domain would not fit ``|q| < 2**30``.
     """
     lo = coords.min(axis=0)
     hi = coords.max(axis=0)
     origin = (lo + hi) / 2
     half = float(np.max(hi - lo) / 2)
-    if half <= 0.0:
-        half = 1.0
-    step = 2.0 ** (int(np.ceil(np.log2(half))) - 29)
-    return origin.astype(np.float64), step
+    ext = float(extent) if extent > 0 else max(half, 1.0)
+    k = int(np.ceil(np.log2(ext))) - 21
+    if half > 0:
+        k = max(k, int(np.ceil(np.log2(half))) - 29)
+    return origin.astype(np.float64), 2.0 ** k
 
 
 class Integrator(ABC):
@@ -367,7 +371,13 @@ class _CUDAIntegrator(Integrator):
             self.vel_d = self.acc_d = self.rho32_d = None
         self.sc32_d = (None if self.stiffness_corrections_d is None
                        else self._empty((n, mn), torch.float32))
-        self.pos_origin, self.pos_scale = _pos_frame(self.coords)
+        self.nflags_d = self._empty((n,), torch.int32)
+        ext = self._zeros((1,), torch.float64)
+        check(lib().pp_bond_extent(_ptr(self.nlist_d), _ptr(self.r0_d), n, mn,
+                                   _ptr(ext), self._stream), "pp_bond_extent")
+        self.bond_extent = float(ext.cpu().item())
+        self.pos_origin, self.pos_scale = _pos_frame(self.coords,
+                                                     self.bond_extent)
 
     def _make_fused_args(self):
         a = _lib.FusedArgs()
@@ -419,6 +429,7 @@ class _CUDAIntegrator(Integrator):
             a.frc = _ptr(self.frc_d)
             a.rho32 = _ptr(self.rho32_d)
             a.sc32 = _ptr(self.sc32_d)
+            a.nflags = _ptr(self.nflags_d)
             a.pos_scale = float(self.pos_scale)
             for k in range(3):
                 a.pos_origin[k] = float(self.pos_origin[k])

@@ -109,9 +109,23 @@ def test_fixed_point_frame_exact_differences():
     from probabilistic_peridynamics_gb300.integrators import _pos_frame
     rng = np.random.default_rng(0)
     coords = rng.uniform(-3.0, 5.0, size=(1000, 3))
-    origin, step = _pos_frame(coords)
+    extent = 0.3
+    origin, step = _pos_frame(coords, extent)
     assert np.log2(step) == int(np.log2(step))  # a power of two
+    assert extent / step <= 2 ** 21
     q = np.rint((coords - origin) / step)
-    assert np.all(np.abs(q) <= 2 ** 29)
-    # reconstruction error below one step, differences exact integers
+    assert np.all(np.abs(q) < 2 ** 30)
     assert np.all(np.abs(origin + q * step - coords) <= step / 2)
+    # bonds no longer than the extent give |dq| < 2**22: exact in float
+    dq = np.abs(q[1:] - q[:-1])
+    short = np.all(np.abs(coords[1:] - coords[:-1]) <= extent, axis=1)
+    assert np.all(dq[short] < 2 ** 22)
+
+
+def test_magic_conversion_exact():
+    """float(q) = bits(0x4B400000 + q) - 1.5*2**23 for |q| < 2**22."""
+    q = np.array([-(2 ** 22) + 1, -12345, -1, 0, 1, 777, 2 ** 22 - 1],
+                 dtype=np.int32)
+    bits = (q + np.int32(0x4B400000)).astype(np.int32)
+    f = bits.view(np.float32).astype(np.float64) - 12582912.0
+    assert np.array_equal(f, q.astype(np.float64))
