@@ -95,7 +95,8 @@ def test_validation_without_gpu(L):
     buf = (ctypes.c_char * 64)()
     base = ctypes.addressof(buf)
     for name in ("r0", "vols", "family", "bc_types", "bc_values",
-                 "fc_types", "fc_values", "nlist", "n_neigh", "frc"):
+                 "fc_types", "fc_values", "nlist", "n_neigh", "frc",
+                 "nflags"):
         setattr(fa, name, base)
     fa.precision = _lib.PP_MIXED
     fa.pos_q = base + 4
