@@ -504,6 +504,8 @@ def main():
     ms_per_step = ms / args.steps
     value = world * w["bonds"] * args.steps / (ms * 1e-3)
     kernel_ms = time_kernel_launches(integ, 200, torch)
+    tuning = integ.tuning
+    variant = int(integ._fargs.variant)
     launches = args.steps + (args.steps // 16 + 1
                              if args.steps >= 32 else 0)
     del integ
@@ -521,7 +523,9 @@ def main():
 
     variants = {"fused_mixed": {"bond_updates_per_s": value,
                                 "ms_per_step": ms_per_step,
-                                "kernel_ms": kernel_ms}}
+                                "kernel_ms": kernel_ms,
+                                "autotune_ms": tuning,
+                                "variant": variant}}
     for name, precision, fused in (("plain_fp64", "float64", False),
                                    ("fused_fp64", "float64", True)):
         it = make_integrator(w, precision, fused, context=ctx)

@@ -46,6 +46,9 @@ extern "C" {
 #define PP_MIXED                    1  /* FP32 bonds, exact FP64 stretch test,
                                           double-float node state          */
 
+/* Number of PP_MIXED kernel variants (pp_fused_args.variant). */
+#define PP_MIXED_VARIANTS           2
+
 /* Flags of the fused step. */
 #define PP_FLAG_COMPENSATED         1  /* compensated (TwoSum) FP32 force sum */
 
@@ -170,7 +173,11 @@ typedef struct pp_fused_args {
     int32_t nregimes;
     int32_t nbond_types;
     int32_t flags;
-    int32_t nodes_per_block;       /* warps per block; 0 = default (8)     */
+    int32_t nodes_per_block;       /* PP_FLOAT64: warps per block (0 = 8)  */
+    int32_t variant;               /* PP_MIXED kernel variant, 0..PP_MIXED_VARIANTS-1:
+                                      register budget for 2 (0) or 3 (1)
+                                      resident CTAs per SM               */
+    int32_t reserved;              /* must be 0                            */
     double dt;
     double damping;
     double bond_stiffness;         /* scalar when bond_types == NULL       */

@@ -27,6 +27,7 @@ PP_FLOAT64 = 0
 PP_MIXED = 1
 
 PP_FLAG_COMPENSATED = 1
+PP_MIXED_VARIANTS = 2
 
 _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
@@ -56,7 +57,8 @@ class FusedArgs(ctypes.Structure):
     _fields_ = [
         ("nnodes", _i32), ("max_neigh", _i32), ("integrator", _i32),
         ("precision", _i32), ("nregimes", _i32), ("nbond_types", _i32),
-        ("flags", _i32), ("nodes_per_block", _i32),
+        ("flags", _i32), ("nodes_per_block", _i32), ("variant", _i32),
+        ("reserved", _i32),
         ("dt", _f64), ("damping", _f64), ("bond_stiffness", _f64),
         ("critical_stretch", _f64),
         ("bond_stiffness_table", _vp), ("critical_stretch_table", _vp),

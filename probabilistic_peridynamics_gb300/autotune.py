@@ -1,0 +1,88 @@
+"""Kernel-variant autotuner.
+
+Times each candidate launch configuration of a kernel on the problem it will
+run (CUDA events on the integrator's stream) and keeps the fastest.  The
+candidates run on scratch copies of every array the step writes, so tuning
+never changes the simulation state.  Results are cached per process by a
+problem key.
+"""
+import ctypes
+
+from . import _lib
+from ._lib import check, lib
+
+_cache = {}
+
+
+def time_launches(launch, stream, warmup=3, reps=10):
+    """Mean milliseconds of ``launch()`` over ``reps`` launches."""
+    import torch
+    for _ in range(warmup):
+        launch()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(reps):
+        launch()
+    stop.record(stream)
+    stop.synchronize()
+    return start.elapsed_time(stop) / reps
+
+
+#: FusedArgs fields a mixed-precision step writes.
+_MIXED_WRITES = ("nlist", "regimes", "vel", "acc", "frc", "n_neigh")
+
+
+def tune_mixed(integ, warmup=3, reps=10):
+    """Pick ``FusedArgs.variant`` for a mixed-precision integrator.
+
+    :returns: dict variant -> milliseconds per step; sets
+        ``integ._fargs.variant`` to the fastest.
+    """
+    import torch
+    fa = integ._fargs
+    key = ("mixed", fa.nnodes, fa.max_neigh, fa.integrator,
+           bool(fa.stiffness_corrections), bool(fa.bond_types), fa.flags)
+    if key in _cache:
+        fa.variant = _cache[key][0]
+        return _cache[key][1]
+    scratch = _lib.FusedArgs()
+    ctypes.pointer(scratch)[0] = fa  # copy all fields
+    keep = []
+
+    def clone(ptr_value, tensor):
+        if not ptr_value or tensor is None:
+            return ptr_value
+        t = tensor.clone()
+        keep.append(t)
+        return t.data_ptr()
+
+    tensors = {"nlist": integ.nlist_d, "regimes": integ.regimes_d,
+               "vel": integ.vel_d, "acc": integ.acc_d, "frc": integ.frc_d,
+               "n_neigh": integ.n_neigh_d}
+    with integ.context.on_stream():
+        for name in _MIXED_WRITES:
+            setattr(scratch, name, clone(getattr(scratch, name),
+                                         tensors[name]))
+        for k in range(2):
+            scratch.uhi[k] = clone(scratch.uhi[k], integ.uhi_d[k])
+            scratch.ulo[k] = clone(scratch.ulo[k], integ.ulo_d[k])
+        results = {}
+        stream = integ.context.stream
+        for variant in range(_lib.PP_MIXED_VARIANTS):
+            scratch.variant = variant
+            parity = [integ._parity]
+
+            def launch():
+                check(lib().pp_fused_step(ctypes.byref(scratch), parity[0],
+                                          0.0, 0.0, integ._stream),
+                      "pp_fused_step")
+                parity[0] ^= 1
+            results[variant] = time_launches(launch, stream, warmup, reps)
+        stream.synchronize()
+    del keep
+    best = min(results, key=results.get)
+    fa.variant = best
+    _cache[key] = (best, results)
+    torch.cuda.empty_cache()
+    return results

@@ -93,6 +93,7 @@ int validate(const pp_fused_args& a) {
     if (!is_pow2_le_1024(a.max_neigh)) return PP_ERROR_MAX_NEIGH;
     if (a.integrator < PP_EULER || a.integrator > PP_VELOCITY_VERLET) return PP_ERROR_INVALID_VALUE;
     if (a.nodes_per_block < 0 || a.nodes_per_block > 32) return PP_ERROR_INVALID_VALUE;
+    if (a.reserved != 0) return PP_ERROR_INVALID_VALUE;
     if (a.nnodes == 0) return PP_SUCCESS;
     if (!a.r0 || !a.vols || !a.family || !a.bc_types || !a.bc_values || !a.fc_types ||
         !a.fc_values || !a.nlist || !a.n_neigh)

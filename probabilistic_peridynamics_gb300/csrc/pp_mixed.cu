@@ -38,6 +38,7 @@ namespace {
 constexpr int kWarps = 8;
 constexpr int kChunk = 64;  // nodes per CTA
 constexpr int kMaxTable = 256;
+
 constexpr int kMagicI = 0x4B400000;  // bit pattern of 1.5 * 2^23
 constexpr float kMagicF = 12582912.0f;
 
@@ -96,6 +97,53 @@ __device__ __forceinline__ Bond32 bond32(const int4& qi, const float4& ui, const
     return b;
 }
 
+// Two bonds (i -> a, i -> b) at once in packed FP32x2 arithmetic (.x = a,
+// .y = b); the same operations and error band as bond32.
+struct Bond32x2 {
+    float2 px, py, pz, s, ry, band;
+};
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+
+__device__ __forceinline__ Bond32x2 bond32x2(const int4& qi, const float4& ui, const int4& qa,
+                                             const float4& ua, const int4& qb,
+                                             const float4& ub, const MixedConst& c) {
+    const float2 H = f2(c.h), MH = f2(c.mh);
+    const float2 xx = __ffma2_rn(
+        f2(__int_as_float(qa.x - qi.x + kMagicI), __int_as_float(qb.x - qi.x + kMagicI)), H, MH);
+    const float2 xy = __ffma2_rn(
+        f2(__int_as_float(qa.y - qi.y + kMagicI), __int_as_float(qb.y - qi.y + kMagicI)), H, MH);
+    const float2 xz = __ffma2_rn(
+        f2(__int_as_float(qa.z - qi.z + kMagicI), __int_as_float(qb.z - qi.z + kMagicI)), H, MH);
+    const float2 ex = f2(ua.x - ui.x, ub.x - ui.x);
+    const float2 ey = f2(ua.y - ui.y, ub.y - ui.y);
+    const float2 ez = f2(ua.z - ui.z, ub.z - ui.z);
+    Bond32x2 b;
+    b.px = __fadd2_rn(xx, ex);
+    b.py = __fadd2_rn(xy, ey);
+    b.pz = __fadd2_rn(xz, ez);
+    const float2 mx = __fadd2_rn(b.px, xx), my = __fadd2_rn(b.py, xy), mz = __fadd2_rn(b.pz, xz);
+    const float2 xi2 = __ffma2_rn(xx, xx, __ffma2_rn(xy, xy, __fmul2_rn(xz, xz)));
+    const float2 y2 = __ffma2_rn(b.px, b.px, __ffma2_rn(b.py, b.py, __fmul2_rn(b.pz, b.pz)));
+    const float2 num = __ffma2_rn(ex, mx, __ffma2_rn(ey, my, __fmul2_rn(ez, mz)));
+    const float2 rxi = f2(rsqrtf(xi2.x), rsqrtf(xi2.y));
+    b.ry = f2(rsqrtf(y2.x), rsqrtf(y2.y));
+    const float2 lsum = __ffma2_rn(y2, b.ry, __fmul2_rn(xi2, rxi));
+    const float2 rl = f2(__fdividef(1.0f, lsum.x), __fdividef(1.0f, lsum.y));
+    b.s = __fmul2_rn(__fmul2_rn(num, rxi), rl);
+    const float2 einf = f2(fmaxf(fabsf(ex.x), fmaxf(fabsf(ey.x), fabsf(ez.x))),
+                           fmaxf(fabsf(ex.y), fmaxf(fabsf(ey.y), fabsf(ez.y))));
+    const float2 r = __fmul2_rn(einf, __fmul2_rn(rxi, f2(1.7320508f)));
+    const float2 t2 = __ffma2_rn(f2(2.0f), r, f2(fabsf(b.s.x), fabsf(b.s.y)));
+    const float2 geo = __ffma2_rn(f2(c.geo), rxi, f2(1.1e-7f));
+    const float2 uw = __fadd2_rn(f2(ui.w + ua.w, ui.w + ub.w), einf);
+    const float2 uterm = __fmul2_rn(__fmul2_rn(f2(1.1e-7f), uw), rxi);
+    const float2 arith = __fmul2_rn(f2(1.0e-6f), __ffma2_rn(r, r, t2));
+    b.band = __ffma2_rn(f2(2.0f), __ffma2_rn(geo, t2, __fadd2_rn(uterm, arith)), f2(1.0e-12f));
+    return b;
+}
+
 // Binary64 stretch of bond (i, j) from the reference r0 and the exact
 // double-float displacement, in the reference operation order
 // (peridynamics.cl:65-75).
@@ -150,8 +198,8 @@ __device__ __forceinline__ float reduce4(float x, float y, float z, float w, int
     return v;
 }
 
-template <int SL, bool CORR, bool TYPES>
-__global__ void __launch_bounds__(kWarps * 32)
+template <int SL, bool CORR, bool TYPES, int MINB>
+__global__ void __launch_bounds__(kWarps * 32, MINB)
     k_mixed(pp_fused_args a, MixedConst c, int parity, Launch l) {
     __shared__ float4 s_frc[kChunk];
     __shared__ float s_thr[TYPES ? kMaxTable : 1];
@@ -193,9 +241,15 @@ __global__ void __launch_bounds__(kWarps * 32)
         int bt[SL], rg[SL];
 #pragma unroll
         for (int k = 0; k < SL; ++k) {
-            const int j = jr[k] != -1 ? jr[k] : i;
-            qj[k] = ldg_i4(a.pos_q, j);
-            uj[k] = ldg_f4(uhi, j);
+            // An empty slot gets a harmless stand-in (one fixed-point step
+            // away, same displacement) so that all arithmetic stays finite.
+            if (jr[k] != -1) {
+                qj[k] = ldg_i4(a.pos_q, jr[k]);
+                uj[k] = ldg_f4(uhi, jr[k]);
+            } else {
+                qj[k] = make_int4(qi.x + 1, qi.y, qi.z, 0);
+                uj[k] = ui;
+            }
             const int64_t gid = row + lane + 32 * k;
             if constexpr (CORR) sc[k] = jr[k] != -1 ? __ldcs(a.sc32 + gid) : 0.f;
             if constexpr (TYPES) {
@@ -206,46 +260,67 @@ __global__ void __launch_bounds__(kWarps * 32)
         float sx = 0.f, sy = 0.f, sz = 0.f;
         float cnt = 0.f;
         unsigned amb = 0u;
-#pragma unroll
-        for (int k = 0; k < SL; ++k) {
-            if (jr[k] == -1) continue;
+        // Decide one bond from its FP32 stretch; returns the force factor
+        // (force = factor * p) or 0.  Ambiguous slots are deferred.
+        auto decide = [&](int k, float s, float band, float ry) -> float {
+            if (jr[k] == -1) return 0.0f;
             const int64_t gid = row + lane + 32 * k;
-            const Bond32 b = bond32(qi, ui, qj[k], uj[k], c);
             float w = __int_as_float(qj[k].w);  // k*vol (PMB) or vol (types)
             bool intact;
             if constexpr (!TYPES) {
-                const float d = b.s - c.s0;
-                if (!(fabsf(d) > b.band + c.s0_err)) {
+                const float d = s - c.s0;
+                if (!(fabsf(d) > band + c.s0_err)) {
                     amb |= 1u << k;
-                    continue;
+                    return 0.0f;
                 }
                 intact = d < 0.0f;
+                w *= s;
             } else {
                 bool ambiguous = false;
                 const int reg = next_regime(rg[k], bt[k], nr, [&](int idx) {
                     const float thr = s_thr[idx];
-                    const float d = b.s - thr;
-                    if (!(fabsf(d) > b.band + 6.0e-8f * fabsf(thr))) ambiguous = true;
+                    const float d = s - thr;
+                    if (!(fabsf(d) > band + 6.0e-8f * fabsf(thr))) ambiguous = true;
                     return d < 0.0f;
                 });
                 if (ambiguous) {
                     amb |= 1u << k;
-                    continue;
+                    return 0.0f;
                 }
                 if (reg != rg[k]) a.regimes[gid] = reg;
                 intact = reg < nr;
-                if (intact) w *= fmaf(b.s, s_k[bt[k] + reg], s_c[bt[k] + reg]);
+                if (intact) w *= fmaf(s, s_k[bt[k] + reg], s_c[bt[k] + reg]);
             }
             if (!intact) {
                 a.nlist[gid] = -1;
-                continue;
+                return 0.0f;
             }
-            float fv = TYPES ? w * b.ry : b.s * w * b.ry;
-            if constexpr (CORR) fv *= sc[k];
-            sx = fmaf(fv, b.px, sx);
-            sy = fmaf(fv, b.py, sy);
-            sz = fmaf(fv, b.pz, sz);
+            if constexpr (CORR) w *= sc[k];
             cnt += 1.0f;
+            return w * ry;
+        };
+        if constexpr (SL == 1) {
+            const Bond32 b = bond32(qi, ui, qj[0], uj[0], c);
+            const float fv = decide(0, b.s, b.band, b.ry);
+            sx = fv * b.px;
+            sy = fv * b.py;
+            sz = fv * b.pz;
+        } else {
+            float2 ax = f2(0.0f), ay = f2(0.0f), az = f2(0.0f);
+#pragma unroll
+            for (int k = 0; k < SL / 2; ++k) {
+                const int kb = k + SL / 2;
+                if (jr[k] == -1 && jr[kb] == -1) continue;
+                const Bond32x2 b = bond32x2(qi, ui, qj[k], uj[k], qj[kb], uj[kb], c);
+                const float2 fv = f2(decide(k, b.s.x, b.band.x, b.ry.x),
+                                     decide(kb, b.s.y, b.band.y, b.ry.y));
+                ax = __ffma2_rn(fv, b.px, ax);
+                ay = __ffma2_rn(fv, b.py, ay);
+                az = __ffma2_rn(fv, b.pz, az);
+            }
+            sx = ax.x + ax.y;
+            sy = ay.x + ay.y;
+            sz = az.x + az.y;
         }
         // Slow path: slots whose FP32 stretch is too close to a critical
         // stretch are decided on the binary64 stretch.
@@ -366,7 +441,11 @@ MixedConst mixed_const(const pp_fused_args& a) {
 template <int SL, bool CORR, bool TYPES>
 void launch_variant(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
     const dim3 grid((a.nnodes + kChunk - 1) / kChunk), block(kWarps * 32);
-    k_mixed<SL, CORR, TYPES><<<grid, block, 0, st>>>(a, mixed_const(a), parity, l);
+    // variant 0: register budget for 2 resident CTAs per SM, 1: for 3.
+    if (a.variant == 1)
+        k_mixed<SL, CORR, TYPES, 3><<<grid, block, 0, st>>>(a, mixed_const(a), parity, l);
+    else
+        k_mixed<SL, CORR, TYPES, 2><<<grid, block, 0, st>>>(a, mixed_const(a), parity, l);
 }
 
 template <int SL>
@@ -474,6 +553,7 @@ int validate_mixed(const pp_fused_args& a) {
     if (a.stiffness_corrections && !a.sc32) return PP_ERROR_INVALID_VALUE;
     if (a.bond_types && a.nbond_types * a.nregimes > kMaxTable) return PP_ERROR_UNSUPPORTED;
     if (!(a.pos_scale > 0.0)) return PP_ERROR_INVALID_VALUE;
+    if (a.variant < 0 || a.variant >= PP_MIXED_VARIANTS) return PP_ERROR_INVALID_VALUE;
     return PP_SUCCESS;
 }
 

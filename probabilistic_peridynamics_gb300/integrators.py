@@ -167,7 +167,8 @@ class _CUDAIntegrator(Integrator):
     _dynamic = False      # needs densities, ud, udd
 
     def __init__(self, dt, context=None, fused=True, precision="float64",
-                 compensated=False, nodes_per_block=0, use_graph=True):
+                 compensated=False, nodes_per_block=0, use_graph=True,
+                 autotune=True):
         super().__init__(dt, context)
         if precision not in ("float64", "mixed"):
             raise ValueError("precision must be 'float64' or 'mixed' "
@@ -180,6 +181,8 @@ class _CUDAIntegrator(Integrator):
         self.compensated = bool(compensated)
         self.nodes_per_block = int(nodes_per_block)
         self.use_graph = bool(use_graph)
+        self.autotune = bool(autotune)
+        self.tuning = None
         self.damping = 0.0
         self._parity = 0
         self._fargs = None
@@ -354,6 +357,9 @@ class _CUDAIntegrator(Integrator):
         if self.precision == "mixed":
             check(lib().pp_mixed_pack(ctypes.byref(self._fargs), 0,
                                       self._stream), "pp_mixed_pack")
+            if self.autotune:
+                from .autotune import tune_mixed
+                self.tuning = tune_mixed(self)
         self._create_special_buffers()
 
     def _create_mixed_buffers(self):

@@ -53,11 +53,12 @@ def test_struct_layout_matches_header():
     from probabilistic_peridynamics_gb300 import _lib
     # pp_bond_force_args: 4 int32, 14 pointers, 3 doubles
     assert ctypes.sizeof(_lib.BondForceArgs) == 4 * 4 + 14 * 8 + 3 * 8
-    # pp_fused_args: 8 int32, 4 doubles, 45-8=... counted field by field
+    # pp_fused_args: 10 int32 then doubles and pointers
     f = dict((n, getattr(_lib.FusedArgs, n)) for n, _ in
              _lib.FusedArgs._fields_)
-    assert f["dt"].offset == 32
-    assert f["bond_stiffness_table"].offset == 64
+    assert f["variant"].offset == 32
+    assert f["dt"].offset == 40
+    assert f["bond_stiffness_table"].offset == 72
     assert f["pos_origin"].offset + 24 == ctypes.sizeof(_lib.FusedArgs)
 
 
