@@ -93,7 +93,9 @@ def profile_case(which):
     import torch
     w = build_workload()
     precision = "mixed" if which == "mixed" else "float64"
-    integ = make_integrator(w, precision, which != "plain")
+    integ = make_integrator(w, precision, which != "plain", autotune=False)
+    if which == "mixed":
+        integ._fargs.variant = int(os.environ.get("PP_PROFILE_VARIANT", "1"))
     for k in range(6):
         integ(PULL_RATE * (k + 1), 0.0)
     integ.context.stream.synchronize()
@@ -124,10 +126,11 @@ def build_workload(pow2=True):
                 bonds=int(family.sum()), crack_pairs=int(len(pairs)))
 
 
-def make_integrator(w, precision, fused, context=None):
+def make_integrator(w, precision, fused, context=None, autotune=True):
     import probabilistic_peridynamics_gb300 as pp
     integ = pp.VelocityVerletCUDA(DAMPING, dt=DT, precision=precision,
-                                  fused=fused, context=context)
+                                  fused=fused, context=context,
+                                  autotune=autotune)
     integ.build(w["nnodes"], 3, w["max_neigh"], w["coords"], w["volume"],
                 w["family"], w["bc_types"], w["bc_values"],
                 w["force_bc_types"], w["force_bc_values"], None, None,

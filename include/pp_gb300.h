@@ -49,6 +49,11 @@ extern "C" {
 /* Number of PP_MIXED kernel variants (pp_fused_args.variant). */
 #define PP_MIXED_VARIANTS           2
 
+/* Values of pp_fused_args.status after a step (read by the caller). */
+#define PP_STATUS_OK                0
+#define PP_STATUS_COPY_TIMEOUT      1  /* a bulk copy did not complete: the
+                                          step's results are invalid     */
+
 /* Flags of the fused step. */
 #define PP_FLAG_COMPENSATED         1  /* compensated (TwoSum) FP32 force sum */
 
@@ -157,7 +162,10 @@ int pp_update_displacement_velocity_verlet(
 /*   nflags  (nnodes) int: bit d set when bc_types[3i+d] != 0, bit 3+d when  */
 /*           fc_types[3i+d] != 0                                            */
 /*   sc32    (nnodes,max_neigh) float stiffness corrections or NULL         */
-/* and reads the reference r0 (f64) and the double-float displacement only  */
+/* umax and status are caller-allocated device words (zero-initialised by   */
+/* pp_mixed_pack / the caller) that the step reads and updates.             */
+/* The step reads the reference r0 (f64) and the double-float displacement  */
+/* only                                                                     */
 /* for bonds whose FP32 stretch lies within a proven error band of a        */
 /* critical stretch; there the break/regime decision is taken from the      */
 /* binary64 stretch formula of peridynamics.cl:65-75, so it is the          */
@@ -217,7 +225,11 @@ typedef struct pp_fused_args {
     float* rho32;                  /* (nnodes) float4 densities (EC / VV)  */
     float* sc32;
     int32_t* nflags;               /* (nnodes) boundary-condition flags    */
+    float* umax;                   /* device word: running max of |u| (scratch) */
+    int32_t* status;               /* device word: 0, or PP_STATUS_* set by a
+                                      kernel that gave up waiting (scratch) */
     double pos_scale;
+    double min_bond;               /* smallest |xi| over the bonds (pp_bond_extent) */
     double pos_origin[3];
 } pp_fused_args;
 
@@ -238,9 +250,10 @@ int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t nsteps,
                  int64_t first, int32_t use_graph, int32_t chunk,
                  int64_t* step_base, void* stream);
 
-/* Largest |r0[j][d] - r0[i][d]| over the bonds (i, j) of nlist (entries
- * != -1) and the three components d, written to *extent (a caller-allocated
- * device double).  The caller derives pos_scale for PP_MIXED from it. */
+/* Over the bonds (i, j) of nlist (entries != -1): extent[0] = the largest
+ * |r0[j][d] - r0[i][d]| over the three components d, extent[1] = the
+ * smallest |r0[j] - r0[i]|; extent is two caller-allocated device doubles.
+ * The caller derives pos_scale and min_bond for PP_MIXED from them. */
 int pp_bond_extent(const int32_t* nlist, const double* r0, int32_t nnodes,
                    int32_t max_neigh, double* extent, void* stream);
 

@@ -28,6 +28,8 @@ PP_MIXED = 1
 
 PP_FLAG_COMPENSATED = 1
 PP_MIXED_VARIANTS = 2
+PP_STATUS_OK = 0
+PP_STATUS_COPY_TIMEOUT = 1
 
 _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
@@ -72,7 +74,8 @@ class FusedArgs(ctypes.Structure):
         ("body_force", _vp), ("n_neigh", _vp), ("damage", _vp),
         ("pos_q", _vp), ("uhi", _vp * 2), ("ulo", _vp * 2), ("vel", _vp),
         ("acc", _vp), ("frc", _vp), ("rho32", _vp), ("sc32", _vp),
-        ("nflags", _vp), ("pos_scale", _f64), ("pos_origin", _f64 * 3),
+        ("nflags", _vp), ("umax", _vp), ("status", _vp),
+        ("pos_scale", _f64), ("min_bond", _f64), ("pos_origin", _f64 * 3),
     ]
 
 

@@ -30,7 +30,8 @@ def time_launches(launch, stream, warmup=3, reps=10):
 
 
 #: FusedArgs fields a mixed-precision step writes.
-_MIXED_WRITES = ("nlist", "regimes", "vel", "acc", "frc", "n_neigh")
+_MIXED_WRITES = ("nlist", "regimes", "vel", "acc", "frc", "n_neigh", "umax",
+                 "status")
 
 
 def tune_mixed(integ, warmup=3, reps=10):
@@ -59,7 +60,8 @@ def tune_mixed(integ, warmup=3, reps=10):
 
     tensors = {"nlist": integ.nlist_d, "regimes": integ.regimes_d,
                "vel": integ.vel_d, "acc": integ.acc_d, "frc": integ.frc_d,
-               "n_neigh": integ.n_neigh_d}
+               "n_neigh": integ.n_neigh_d, "umax": integ.umax_d,
+               "status": integ.status_d}
     with integ.context.on_stream():
         for name in _MIXED_WRITES:
             setattr(scratch, name, clone(getattr(scratch, name),

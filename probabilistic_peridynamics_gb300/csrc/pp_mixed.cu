@@ -31,6 +31,7 @@
 // the binary64 slow path is unaffected by those flags.
 #include "pp_bond_f64.cuh"
 #include "pp_fused.cuh"
+#include "pp_tma.cuh"
 
 namespace pp {
 namespace {
@@ -43,11 +44,12 @@ constexpr int kMagicI = 0x4B400000;  // bit pattern of 1.5 * 2^23
 constexpr float kMagicF = 12582912.0f;
 
 struct MixedConst {
-    float h;       // fixed-point step (a power of two)
-    float mh;      // -kMagicF * h
-    float geo;     // sqrt(3) * h: bound on the rounding of each xi
-    float s0;      // critical stretch (PMB), rounded to float
-    float s0_err;  // 6e-8 * |s0|: rounding of s0 to float
+    float h;        // fixed-point step (a power of two)
+    float mh;       // -kMagicF * h
+    float geo;      // sqrt(3) * h: bound on the rounding of each xi
+    float rxi_max;  // 1 / (smallest bond length)
+    float s0;       // critical stretch (PMB), rounded to float
+    float s0_err;   // 6e-8 * |s0|: rounding of s0 to float
     float dt_hi, dt_lo;
     float half_hi, half_lo;
     float damping;
@@ -58,7 +60,7 @@ struct Bond32 {
     float px, py, pz;  // deformed bond vector
     float s;           // stretch
     float ry;          // 1 / |p|
-    float band;        // bound on |s - s64|
+    float rxi;         // 1 / |xi|
 };
 
 __device__ __forceinline__ float fixed_diff(int qj, int qi, const MixedConst& c) {
@@ -79,69 +81,47 @@ __device__ __forceinline__ Bond32 bond32(const int4& qi, const float4& ui, const
     const float xi2 = fmaf(xx, xx, fmaf(xy, xy, xz * xz));
     const float y2 = fmaf(b.px, b.px, fmaf(b.py, b.py, b.pz * b.pz));
     const float num = fmaf(ex, mx, fmaf(ey, my, ez * mz));  // |p|^2 - |xi|^2
-    const float rxi = rsqrtf(xi2);
+    b.rxi = rsqrtf(xi2);
     b.ry = rsqrtf(y2);
-    const float lsum = fmaf(y2, b.ry, xi2 * rxi);  // |p| + |xi|
-    b.s = __fdividef(num * rxi, lsum);
-    // Error band against the binary64 stretch of the same state:
-    //   geometry (fixed-point rounding of xi), displacement rounding to
-    //   float, FP32 arithmetic (<= 1e-6 relative), safety factor 2.
-    const float einf = fmaxf(fabsf(ex), fmaxf(fabsf(ey), fabsf(ez)));
-    const float r = 1.7320508f * einf * rxi;  // >= |e| / |xi|
-    const float as = fabsf(b.s);
-    const float t2 = fmaf(2.0f, r, as);                          // 2r + |s|
-    const float geo = fmaf(c.geo, rxi, 1.1e-7f);                 // |dxi|/|xi|
-    const float uterm = 1.1e-7f * (ui.w + uj.w + einf) * rxi;    // float u
-    const float arith = 1.0e-6f * fmaf(r, r, t2);                // 2r + r^2 + |s|
-    b.band = fmaf(2.0f, fmaf(geo, t2, uterm + arith), 1.0e-12f);
+    const float lsum = fmaf(y2, b.ry, xi2 * b.rxi);  // |p| + |xi|
+    // s = (|p| - |xi|)/|xi| without cancellation: (2 xi.e + e.e)/(|xi|(|p|+|xi|))
+    b.s = __fdividef(num * b.rxi, lsum);
     return b;
 }
 
-// Two bonds (i -> a, i -> b) at once in packed FP32x2 arithmetic (.x = a,
-// .y = b); the same operations and error band as bond32.
-struct Bond32x2 {
-    float2 px, py, pz, s, ry, band;
+// Bound on |s - s64| for one bond: s64 is the binary64 stretch of the same
+// state (reference formula).  Terms: geometry (fixed-point rounding of xi,
+// <= sqrt(3) h per bond vector), the rounding of the displacement to float
+// (<= 2^-24 |u| per component), FP32 arithmetic (<= 1e-6 relative, which
+// covers the approximate rsqrt and division), times a safety factor 2.
+__device__ __forceinline__ float band32(const float4& ui, const float4& uj, const Bond32& b,
+                                        const MixedConst& c) {
+    const float einf =
+        fmaxf(fabsf(uj.x - ui.x), fmaxf(fabsf(uj.y - ui.y), fabsf(uj.z - ui.z)));
+    const float r = 1.7320508f * einf * b.rxi;  // >= |e| / |xi|
+    const float t2 = fmaf(2.0f, r, fabsf(b.s));
+    const float geo = fmaf(c.geo, b.rxi, 1.1e-7f);
+    const float uterm = 1.1e-7f * (ui.w + uj.w + einf) * b.rxi;
+    const float arith = 1.0e-6f * fmaf(r, r, t2);
+    return fmaf(2.0f, fmaf(geo, t2, uterm + arith), 1.0e-12f);
+}
+
+// A bound of band32 valid for every bond of the step, affine in |s|:
+// band32 <= quick_a + quick_c * |s|, from the running max |u| (U) and the
+// shortest bond.  Decides almost every bond with three instructions.
+struct QuickBand {
+    float a, c;
 };
 
-__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
-__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
-
-__device__ __forceinline__ Bond32x2 bond32x2(const int4& qi, const float4& ui, const int4& qa,
-                                             const float4& ua, const int4& qb,
-                                             const float4& ub, const MixedConst& c) {
-    const float2 H = f2(c.h), MH = f2(c.mh);
-    const float2 xx = __ffma2_rn(
-        f2(__int_as_float(qa.x - qi.x + kMagicI), __int_as_float(qb.x - qi.x + kMagicI)), H, MH);
-    const float2 xy = __ffma2_rn(
-        f2(__int_as_float(qa.y - qi.y + kMagicI), __int_as_float(qb.y - qi.y + kMagicI)), H, MH);
-    const float2 xz = __ffma2_rn(
-        f2(__int_as_float(qa.z - qi.z + kMagicI), __int_as_float(qb.z - qi.z + kMagicI)), H, MH);
-    const float2 ex = f2(ua.x - ui.x, ub.x - ui.x);
-    const float2 ey = f2(ua.y - ui.y, ub.y - ui.y);
-    const float2 ez = f2(ua.z - ui.z, ub.z - ui.z);
-    Bond32x2 b;
-    b.px = __fadd2_rn(xx, ex);
-    b.py = __fadd2_rn(xy, ey);
-    b.pz = __fadd2_rn(xz, ez);
-    const float2 mx = __fadd2_rn(b.px, xx), my = __fadd2_rn(b.py, xy), mz = __fadd2_rn(b.pz, xz);
-    const float2 xi2 = __ffma2_rn(xx, xx, __ffma2_rn(xy, xy, __fmul2_rn(xz, xz)));
-    const float2 y2 = __ffma2_rn(b.px, b.px, __ffma2_rn(b.py, b.py, __fmul2_rn(b.pz, b.pz)));
-    const float2 num = __ffma2_rn(ex, mx, __ffma2_rn(ey, my, __fmul2_rn(ez, mz)));
-    const float2 rxi = f2(rsqrtf(xi2.x), rsqrtf(xi2.y));
-    b.ry = f2(rsqrtf(y2.x), rsqrtf(y2.y));
-    const float2 lsum = __ffma2_rn(y2, b.ry, __fmul2_rn(xi2, rxi));
-    const float2 rl = f2(__fdividef(1.0f, lsum.x), __fdividef(1.0f, lsum.y));
-    b.s = __fmul2_rn(__fmul2_rn(num, rxi), rl);
-    const float2 einf = f2(fmaxf(fabsf(ex.x), fmaxf(fabsf(ey.x), fabsf(ez.x))),
-                           fmaxf(fabsf(ex.y), fmaxf(fabsf(ey.y), fabsf(ez.y))));
-    const float2 r = __fmul2_rn(einf, __fmul2_rn(rxi, f2(1.7320508f)));
-    const float2 t2 = __ffma2_rn(f2(2.0f), r, f2(fabsf(b.s.x), fabsf(b.s.y)));
-    const float2 geo = __ffma2_rn(f2(c.geo), rxi, f2(1.1e-7f));
-    const float2 uw = __fadd2_rn(f2(ui.w + ua.w, ui.w + ub.w), einf);
-    const float2 uterm = __fmul2_rn(__fmul2_rn(f2(1.1e-7f), uw), rxi);
-    const float2 arith = __fmul2_rn(f2(1.0e-6f), __ffma2_rn(r, r, t2));
-    b.band = __ffma2_rn(f2(2.0f), __ffma2_rn(geo, t2, __fadd2_rn(uterm, arith)), f2(1.0e-12f));
-    return b;
+__device__ __forceinline__ QuickBand quick_band(float U, const MixedConst& c) {
+    const float geo = fmaf(c.geo, c.rxi_max, 1.1e-7f);
+    const float R = 3.5f * U * c.rxi_max;  // >= sqrt(3) * (|u_i| + |u_j|)(1 + eps) / |xi|
+    QuickBand q;
+    q.a = 2.0f * (geo * 2.0f * R + 1.1e-7f * 4.1f * U * c.rxi_max +
+                  1.0e-6f * fmaf(R, R, 2.0f * R)) +
+          1.0e-12f;
+    q.c = 2.0f * (geo + 1.0e-6f);
+    return q;
 }
 
 // Binary64 stretch of bond (i, j) from the reference r0 and the exact
@@ -169,8 +149,8 @@ __device__ __noinline__ double exact_stretch(const pp_fused_args& a, int parity,
     return ddiv(dsub(y, xi), xi);
 }
 
-// Regime logic of bond_force3/4 (peridynamics.cl:345-367) on an exact
-// decision function lt(threshold index) = (s < critical_stretch[idx]).
+// Regime logic of bond_force3/4 (peridynamics.cl:345-367) on a decision
+// function lt(threshold index) = (s < critical_stretch[idx]).
 // Returns the new regime (>= nregimes means broken).
 template <class Lt>
 __device__ __forceinline__ int next_regime(int reg, int base, int nr, Lt&& lt) {
@@ -198,176 +178,153 @@ __device__ __forceinline__ float reduce4(float x, float y, float z, float w, int
     return v;
 }
 
-template <int SL, bool CORR, bool TYPES, int MINB>
-__global__ void __launch_bounds__(kWarps * 32, MINB)
-    k_mixed(pp_fused_args a, MixedConst c, int parity, Launch l) {
-    __shared__ float4 s_frc[kChunk];
-    __shared__ float s_thr[TYPES ? kMaxTable : 1];
-    __shared__ float s_k[TYPES ? kMaxTable : 1];
-    __shared__ float s_c[TYPES ? kMaxTable : 1];
-    if constexpr (TYPES) {
-        const int nt = a.nbond_types * a.nregimes;
-        for (int t = threadIdx.x; t < nt; t += blockDim.x) {
-            s_thr[t] = (float)a.critical_stretch_table[t];
-            s_k[t] = (float)a.bond_stiffness_table[t];
-            s_c[t] = (float)a.plus_cs[t];
-        }
-        __syncthreads();
-    }
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int node0 = blockIdx.x * kChunk;
+constexpr uint32_t kWaitPolls = 1u << 22;  // bound on mbarrier polls
+
+struct alignas(16) MixedShared {
+    uint64_t bar[2];
+    float4 frc[kChunk];
+    float thr[kMaxTable], k[kMaxTable], c[kMaxTable];
+};
+
+// Bond phase of one node (one warp): returns nothing, parks the reduced
+// (force x, y, z, intact count) of local node li in sh.frc[li].
+template <int SL, bool CORR, bool TYPES>
+__device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const MixedConst& c,
+                                                const QuickBand& qb, MixedShared& sh,
+                                                const int32_t* nl_row, int parity, int i,
+                                                int li, int lane) {
     const int L = a.max_neigh;
     const int nr = a.nregimes;
+    const int64_t row = (int64_t)i * L;
     const float* __restrict__ uhi = a.uhi[parity];
-
-    // ------------------------------------------------------- bond phase
-    for (int t = 0; t < kChunk / kWarps; ++t) {
-        const int li = t * kWarps + warp;
-        const int i = node0 + li;
-        if (i >= a.nnodes) break;  // warp-uniform
-        const int64_t row = (int64_t)i * L;
-        const int4 qi = ldg_i4(a.pos_q, i);
-        const float4 ui = ldg_f4(uhi, i);
-        int jr[SL];
+    const int4 qi = ldg_i4(a.pos_q, i);
+    const float4 ui = ldg_f4(uhi, i);
+    int jr[SL];
+#pragma unroll
+    for (int k = 0; k < SL; ++k) {
+        const int slot = lane + 32 * k;
+        jr[k] = (SL > 1 || slot < L) ? nl_row[slot] : -1;
+    }
+    int4 qj[SL];
+    float4 uj[SL];
+    float sc[SL];
+    int bt[SL], rg[SL];
+#pragma unroll
+    for (int k = 0; k < SL; ++k) {
+        // An empty slot gets a harmless stand-in (one fixed-point step away,
+        // same displacement) so that all arithmetic stays finite.
+        if (jr[k] != -1) {
+            qj[k] = ldg_i4(a.pos_q, jr[k]);
+            uj[k] = ldg_f4(uhi, jr[k]);
+        } else {
+            qj[k] = make_int4(qi.x + 1, qi.y, qi.z, 0);
+            uj[k] = ui;
+        }
+        const int64_t gid = row + lane + 32 * k;
+        if constexpr (CORR) sc[k] = jr[k] != -1 ? __ldcs(a.sc32 + gid) : 0.f;
+        if constexpr (TYPES) {
+            bt[k] = jr[k] != -1 ? __ldcs(a.bond_types + gid) * nr : 0;
+            rg[k] = jr[k] != -1 ? a.regimes[gid] : 0;
+        }
+    }
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    float cnt = 0.f;
+    unsigned amb = 0u;
+#pragma unroll
+    for (int k = 0; k < SL; ++k) {
+        if (jr[k] == -1) continue;
+        const int64_t gid = row + lane + 32 * k;
+        const Bond32 b = bond32(qi, ui, qj[k], uj[k], c);
+        const float quick = fmaf(qb.c, fabsf(b.s), qb.a);
+        float w = __int_as_float(qj[k].w);  // k*vol (PMB) or vol (types)
+        bool intact;
+        if constexpr (!TYPES) {
+            const float d = b.s - c.s0;
+            if (!(fabsf(d) > quick)) {
+                if (!(fabsf(d) > band32(ui, uj[k], b, c) + c.s0_err)) {
+                    amb |= 1u << k;
+                    continue;
+                }
+            }
+            intact = d < 0.0f;
+            w *= b.s;
+        } else {
+            bool ambiguous = false;
+            const int reg = next_regime(rg[k], bt[k], nr, [&](int idx) {
+                const float thr = sh.thr[idx];
+                const float d = b.s - thr;
+                const float err = 6.0e-8f * fabsf(thr);
+                if (!(fabsf(d) > quick + err) &&
+                    !(fabsf(d) > band32(ui, uj[k], b, c) + err))
+                    ambiguous = true;
+                return d < 0.0f;
+            });
+            if (ambiguous) {
+                amb |= 1u << k;
+                continue;
+            }
+            if (reg != rg[k]) a.regimes[gid] = reg;
+            intact = reg < nr;
+            if (intact) w *= fmaf(b.s, sh.k[bt[k] + reg], sh.c[bt[k] + reg]);
+        }
+        if (!intact) {
+            a.nlist[gid] = -1;
+            continue;
+        }
+        float fv = w * b.ry;
+        if constexpr (CORR) fv *= sc[k];
+        sx = fmaf(fv, b.px, sx);
+        sy = fmaf(fv, b.py, sy);
+        sz = fmaf(fv, b.pz, sz);
+        cnt += 1.0f;
+    }
+    // Slow path: slots whose FP32 stretch is too close to a critical stretch
+    // are decided on the binary64 stretch.
+    if (__any_sync(kFull, amb != 0u)) {
 #pragma unroll
         for (int k = 0; k < SL; ++k) {
-            const int slot = lane + 32 * k;
-            jr[k] = (SL > 1 || slot < L) ? __ldcs(a.nlist + row + slot) : -1;
-        }
-        int4 qj[SL];
-        float4 uj[SL];
-        float sc[SL];
-        int bt[SL], rg[SL];
-#pragma unroll
-        for (int k = 0; k < SL; ++k) {
-            // An empty slot gets a harmless stand-in (one fixed-point step
-            // away, same displacement) so that all arithmetic stays finite.
-            if (jr[k] != -1) {
-                qj[k] = ldg_i4(a.pos_q, jr[k]);
-                uj[k] = ldg_f4(uhi, jr[k]);
-            } else {
-                qj[k] = make_int4(qi.x + 1, qi.y, qi.z, 0);
-                uj[k] = ui;
-            }
+            if (!((amb >> k) & 1u)) continue;
             const int64_t gid = row + lane + 32 * k;
-            if constexpr (CORR) sc[k] = jr[k] != -1 ? __ldcs(a.sc32 + gid) : 0.f;
-            if constexpr (TYPES) {
-                bt[k] = jr[k] != -1 ? __ldcs(a.bond_types + gid) * nr : 0;
-                rg[k] = jr[k] != -1 ? a.regimes[gid] : 0;
-            }
-        }
-        float sx = 0.f, sy = 0.f, sz = 0.f;
-        float cnt = 0.f;
-        unsigned amb = 0u;
-        // Decide one bond from its FP32 stretch; returns the force factor
-        // (force = factor * p) or 0.  Ambiguous slots are deferred.
-        auto decide = [&](int k, float s, float band, float ry) -> float {
-            if (jr[k] == -1) return 0.0f;
-            const int64_t gid = row + lane + 32 * k;
-            float w = __int_as_float(qj[k].w);  // k*vol (PMB) or vol (types)
+            const Bond32 b = bond32(qi, ui, qj[k], uj[k], c);
+            const double s64 = exact_stretch(a, parity, i, jr[k]);
+            float w = __int_as_float(qj[k].w);
             bool intact;
             if constexpr (!TYPES) {
-                const float d = s - c.s0;
-                if (!(fabsf(d) > band + c.s0_err)) {
-                    amb |= 1u << k;
-                    return 0.0f;
-                }
-                intact = d < 0.0f;
-                w *= s;
+                intact = s64 < a.critical_stretch;
+                w *= b.s;
             } else {
-                bool ambiguous = false;
                 const int reg = next_regime(rg[k], bt[k], nr, [&](int idx) {
-                    const float thr = s_thr[idx];
-                    const float d = s - thr;
-                    if (!(fabsf(d) > band + 6.0e-8f * fabsf(thr))) ambiguous = true;
-                    return d < 0.0f;
+                    return s64 < a.critical_stretch_table[idx];
                 });
-                if (ambiguous) {
-                    amb |= 1u << k;
-                    return 0.0f;
-                }
                 if (reg != rg[k]) a.regimes[gid] = reg;
                 intact = reg < nr;
-                if (intact) w *= fmaf(s, s_k[bt[k] + reg], s_c[bt[k] + reg]);
+                if (intact) w *= fmaf(b.s, sh.k[bt[k] + reg], sh.c[bt[k] + reg]);
             }
             if (!intact) {
                 a.nlist[gid] = -1;
-                return 0.0f;
+                continue;
             }
-            if constexpr (CORR) w *= sc[k];
+            float fv = w * b.ry;
+            if constexpr (CORR) fv *= sc[k];
+            sx = fmaf(fv, b.px, sx);
+            sy = fmaf(fv, b.py, sy);
+            sz = fmaf(fv, b.pz, sz);
             cnt += 1.0f;
-            return w * ry;
-        };
-        if constexpr (SL == 1) {
-            const Bond32 b = bond32(qi, ui, qj[0], uj[0], c);
-            const float fv = decide(0, b.s, b.band, b.ry);
-            sx = fv * b.px;
-            sy = fv * b.py;
-            sz = fv * b.pz;
-        } else {
-            float2 ax = f2(0.0f), ay = f2(0.0f), az = f2(0.0f);
-#pragma unroll
-            for (int k = 0; k < SL / 2; ++k) {
-                const int kb = k + SL / 2;
-                if (jr[k] == -1 && jr[kb] == -1) continue;
-                const Bond32x2 b = bond32x2(qi, ui, qj[k], uj[k], qj[kb], uj[kb], c);
-                const float2 fv = f2(decide(k, b.s.x, b.band.x, b.ry.x),
-                                     decide(kb, b.s.y, b.band.y, b.ry.y));
-                ax = __ffma2_rn(fv, b.px, ax);
-                ay = __ffma2_rn(fv, b.py, ay);
-                az = __ffma2_rn(fv, b.pz, az);
-            }
-            sx = ax.x + ax.y;
-            sy = ay.x + ay.y;
-            sz = az.x + az.y;
         }
-        // Slow path: slots whose FP32 stretch is too close to a critical
-        // stretch are decided on the binary64 stretch.
-        if (__any_sync(kFull, amb != 0u)) {
-#pragma unroll
-            for (int k = 0; k < SL; ++k) {
-                if (!((amb >> k) & 1u)) continue;
-                const int64_t gid = row + lane + 32 * k;
-                const int j = jr[k];
-                const Bond32 b = bond32(qi, ui, qj[k], uj[k], c);
-                const double s64 = exact_stretch(a, parity, i, j);
-                float w = __int_as_float(qj[k].w);
-                bool intact;
-                if constexpr (!TYPES) {
-                    intact = s64 < a.critical_stretch;
-                } else {
-                    const int reg = next_regime(rg[k], bt[k], nr, [&](int idx) {
-                        return s64 < a.critical_stretch_table[idx];
-                    });
-                    if (reg != rg[k]) a.regimes[gid] = reg;
-                    intact = reg < nr;
-                    if (intact) w *= fmaf(b.s, s_k[bt[k] + reg], s_c[bt[k] + reg]);
-                }
-                if (!intact) {
-                    a.nlist[gid] = -1;
-                    continue;
-                }
-                float fv = TYPES ? w * b.ry : b.s * w * b.ry;
-                if constexpr (CORR) fv *= sc[k];
-                sx = fmaf(fv, b.px, sx);
-                sy = fmaf(fv, b.py, sy);
-                sz = fmaf(fv, b.pz, sz);
-                cnt += 1.0f;
-            }
-        }
-        const float v = reduce4(sx, sy, sz, cnt, lane);
-        if ((lane & 7) == 0) reinterpret_cast<float*>(&s_frc[li])[lane >> 3] = v;
     }
-    __syncthreads();
+    const float v = reduce4(sx, sy, sz, cnt, lane);
+    if ((lane & 7) == 0) reinterpret_cast<float*>(&sh.frc[li])[lane >> 3] = v;
+}
 
-    // ------------------------------------------------------- node phase
+// Node phase of one chunk: thread (node, component) updates one DOF.
+__device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedConst& c,
+                                           const MixedShared& sh, const StepMags& m,
+                                           int parity, int node0) {
     const int li = threadIdx.x >> 2;
     const int comp = threadIdx.x & 3;
     const int i = node0 + li;
     const bool active = i < a.nnodes;
-    const StepMags m = step_mags(l);
-    const float4 fr = s_frc[li];
+    const float4 fr = sh.frc[li];
     const int64_t o4 = 4 * (int64_t)i + comp;
     float hi_new = 0.f, lo_new = 0.f;
     if (active && comp < 3) {
@@ -376,7 +333,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
         const int64_t o3 = 3 * (int64_t)i + comp;
         float frc = body;
         if ((fl >> (3 + comp)) & 1) frc = (float)((double)body + m.force * a.fc_values[o3]);
-        df uu{uhi[o4], a.ulo[parity][o4]};
+        df uu{a.uhi[parity][o4], a.ulo[parity][o4]};
         const df dt{c.dt_hi, c.dt_lo};
         if (a.integrator == PP_EULER) {
             uu = df_add(uu, df_mul_f(dt, frc));
@@ -406,19 +363,102 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
         a.frc[8 * (int64_t)i + comp] = frc;
         a.frc[8 * (int64_t)i + 4 + comp] = body;
     }
-    // max |u| of the node for the next step's error band (quad shuffle)
+    // max |u| of the node (quad shuffle) for the next step's error bounds
     float um = fabsf(hi_new);
     um = fmaxf(um, __shfl_xor_sync(kFull, um, 1));
     um = fmaxf(um, __shfl_xor_sync(kFull, um, 2));
+    um *= 1.0f + 1.2e-7f;
     if (active) {
         if (comp < 3) {
             a.uhi[parity ^ 1][o4] = hi_new;
             a.ulo[parity ^ 1][o4] = lo_new;
         } else {
-            a.uhi[parity ^ 1][o4] = um * (1.0f + 1.2e-7f);
+            a.uhi[parity ^ 1][o4] = um;
             a.ulo[parity ^ 1][o4] = 0.f;
             a.n_neigh[i] = (int)fr.w;
         }
+    }
+    // running max |u| over the whole model (non-negative floats order as ints)
+    const int wmax = __reduce_max_sync(kFull, active ? __float_as_int(um) : 0);
+    if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(reinterpret_cast<int*>(a.umax), wmax);
+}
+
+// One CTA loops over chunks of kChunk nodes.  For SL >= 2 the chunk's
+// neighbour-list rows (contiguous) stream into shared memory by bulk copy,
+// double-buffered one chunk ahead; for SL == 1 they are read in place.
+template <int SL, bool CORR, bool TYPES, int MINB>
+__global__ void __launch_bounds__(kWarps * 32, MINB)
+    k_mixed(pp_fused_args a, MixedConst c, int parity, Launch l) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    MixedShared& sh = *reinterpret_cast<MixedShared*>(smem_raw);
+    int32_t* s_nl = reinterpret_cast<int32_t*>(smem_raw + sizeof(MixedShared));
+    constexpr bool kBulk = SL >= 2;
+    const int L = a.max_neigh;
+    const int nchunks = (a.nnodes + kChunk - 1) / kChunk;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    if constexpr (TYPES) {
+        const int nt = a.nbond_types * a.nregimes;
+        for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+            sh.thr[t] = (float)a.critical_stretch_table[t];
+            sh.k[t] = (float)a.bond_stiffness_table[t];
+            sh.c[t] = (float)a.plus_cs[t];
+        }
+    }
+    uint64_t policy = 0;
+    auto issue = [&](int chunk, int buf) {
+        const int n0 = chunk * kChunk;
+        const int nn = min(kChunk, a.nnodes - n0);
+        const uint32_t bytes = (uint32_t)nn * (uint32_t)L * 4u;
+        mbar_arrive_expect_tx(&sh.bar[buf], bytes);
+        bulk_copy_g2s(s_nl + (size_t)buf * kChunk * L, a.nlist + (int64_t)n0 * L, bytes,
+                      &sh.bar[buf], policy);
+    };
+    if constexpr (kBulk) {
+        if (threadIdx.x == 0) {
+            policy = l2_evict_first_policy();
+            mbar_init(&sh.bar[0], 1);
+            mbar_init(&sh.bar[1], 1);
+            fence_mbar_init();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && (int)blockIdx.x < nchunks) issue(blockIdx.x, 0);
+    } else {
+        __syncthreads();
+    }
+    const StepMags m = step_mags(l);
+    const float U = __ldcg(a.umax);
+    const QuickBand qb = quick_band(U, c);
+    int it = 0;
+    for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x, ++it) {
+        const int buf = it & 1;
+        const int node0 = chunk * kChunk;
+        if constexpr (kBulk) {
+            const int next = chunk + gridDim.x;
+            if (threadIdx.x == 0 && next < nchunks) issue(next, buf ^ 1);
+            const bool ok = mbar_wait_bounded(&sh.bar[buf], (it >> 1) & 1, kWaitPolls);
+            if (__syncthreads_or(!ok)) {
+                // A copy never completed: report, drain the other buffer's
+                // copy (bounded), and leave without touching the state.
+                if (threadIdx.x == 0) {
+                    atomicExch(a.status, PP_STATUS_COPY_TIMEOUT);
+                    if (next < nchunks)
+                        mbar_wait_bounded(&sh.bar[buf ^ 1], ((it + 1) >> 1) & 1, kWaitPolls);
+                }
+                return;
+            }
+        }
+        for (int t = 0; t < kChunk / kWarps; ++t) {
+            const int li = t * kWarps + warp;
+            const int i = node0 + li;
+            if (i >= a.nnodes) break;  // warp-uniform
+            const int32_t* nl_row = kBulk ? s_nl + (size_t)buf * kChunk * L + (size_t)li * L
+                                          : a.nlist + (int64_t)i * L;
+            bond_phase_node<SL, CORR, TYPES>(a, c, qb, sh, nl_row, parity, i, li, lane);
+        }
+        __syncthreads();
+        node_phase(a, c, sh, m, parity, node0);
+        __syncthreads();
     }
 }
 
@@ -427,6 +467,7 @@ MixedConst mixed_const(const pp_fused_args& a) {
     c.h = (float)a.pos_scale;
     c.mh = -kMagicF * c.h;
     c.geo = 1.7320508f * c.h;
+    c.rxi_max = a.min_bond > 0.0 ? (float)(1.0 / a.min_bond) : 3.0e38f;
     c.s0 = (float)a.critical_stretch;
     c.s0_err = 6.0e-8f * fabsf(c.s0);
     c.dt_hi = (float)a.dt;
@@ -438,24 +479,59 @@ MixedConst mixed_const(const pp_fused_args& a) {
     return c;
 }
 
+int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            n = 1;
+    }
+    return n;
+}
+
+// Persistent launch: as many CTAs as fit on the device at once (cached per
+// kernel instance and shared-memory size).
+template <int SL, bool CORR, bool TYPES, int MINB>
+int launch_instance(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
+    auto kernel = k_mixed<SL, CORR, TYPES, MINB>;
+    const size_t smem =
+        sizeof(MixedShared) + (SL >= 2 ? 2 * (size_t)kChunk * a.max_neigh * sizeof(int32_t) : 0);
+    static size_t cached_smem = 0;
+    static int cached_grid = 0;
+    if (cached_smem != smem) {
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return PP_ERROR_CUDA;
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarps * 32, smem) !=
+                cudaSuccess ||
+            per_sm < 1)
+            return PP_ERROR_CUDA;
+        cached_grid = per_sm * sm_count();
+        cached_smem = smem;
+    }
+    const int nchunks = (a.nnodes + kChunk - 1) / kChunk;
+    const int grid = nchunks < cached_grid ? nchunks : cached_grid;
+    kernel<<<grid, kWarps * 32, smem, st>>>(a, mixed_const(a), parity, l);
+    return launch_status();
+}
+
+// variant 0: register budget for 2 resident CTAs per SM, 1: for 3.
 template <int SL, bool CORR, bool TYPES>
-void launch_variant(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
-    const dim3 grid((a.nnodes + kChunk - 1) / kChunk), block(kWarps * 32);
-    // variant 0: register budget for 2 resident CTAs per SM, 1: for 3.
-    if (a.variant == 1)
-        k_mixed<SL, CORR, TYPES, 3><<<grid, block, 0, st>>>(a, mixed_const(a), parity, l);
-    else
-        k_mixed<SL, CORR, TYPES, 2><<<grid, block, 0, st>>>(a, mixed_const(a), parity, l);
+int launch_variant(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
+    if (a.variant == 1) return launch_instance<SL, CORR, TYPES, 3>(a, parity, l, st);
+    return launch_instance<SL, CORR, TYPES, 2>(a, parity, l, st);
 }
 
 template <int SL>
-void launch_sl(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
+int launch_sl(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
     const bool corr = a.stiffness_corrections != nullptr;
     const bool types = a.bond_types != nullptr;
-    if (!corr && !types) launch_variant<SL, false, false>(a, parity, l, st);
-    if (corr && !types) launch_variant<SL, true, false>(a, parity, l, st);
-    if (!corr && types) launch_variant<SL, false, true>(a, parity, l, st);
-    if (corr && types) launch_variant<SL, true, true>(a, parity, l, st);
+    if (!corr && !types) return launch_variant<SL, false, false>(a, parity, l, st);
+    if (corr && !types) return launch_variant<SL, true, false>(a, parity, l, st);
+    if (!corr && types) return launch_variant<SL, false, true>(a, parity, l, st);
+    return launch_variant<SL, true, true>(a, parity, l, st);
 }
 
 // ------------------------------------------------------ pack / export
@@ -484,6 +560,7 @@ __global__ void k_mixed_pack(pp_fused_args a, int parity) {
     }
     a.nflags[i] = fl;
     a.uhi[parity][4 * (int64_t)i + 3] = umax * (1.0f + 1.2e-7f);
+    if (a.umax) atomicMax(reinterpret_cast<int*>(a.umax), __float_as_int(umax * (1.0f + 1.2e-7f)));
     a.ulo[parity][4 * (int64_t)i + 3] = 0.f;
     if (a.vel) {
         for (int d = 0; d < 3; ++d) {
@@ -522,23 +599,38 @@ __global__ void k_mixed_export(pp_fused_args a, int parity) {
     if (a.damage) a.damage[i] = damage_of(a.n_neigh[i], a.family[i]);
 }
 
-__global__ void k_zero_u64(unsigned long long* p) { *p = 0ull; }
+__global__ void k_init_extent(unsigned long long* p) {
+    p[0] = 0ull;                                               // max component
+    p[1] = (unsigned long long)__double_as_longlong(1.0e300);  // min length
+}
 
-// Warp per node: max |r0[j][d] - r0[i][d]| over the row's bonds.
+// Warp per node: max |r0[j][d] - r0[i][d]| and min |r0[j] - r0[i]| over the
+// row's bonds (non-negative doubles order as unsigned integers).
 __global__ void k_bond_extent(const int32_t* __restrict__ nlist, const double* __restrict__ r0,
                               int nnodes, int max_neigh, unsigned long long* out) {
     const int lane = threadIdx.x & 31;
     const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (i >= nnodes) return;
-    double mx = 0.0;
+    double mx = 0.0, mn = 1.0e300;
     for (int k = lane; k < max_neigh; k += 32) {
         const int j = nlist[(int64_t)i * max_neigh + k];
         if (j < 0 || j >= nnodes) continue;
-        for (int d = 0; d < 3; ++d)
-            mx = fmax(mx, fabs(r0[3 * (int64_t)j + d] - r0[3 * (int64_t)i + d]));
+        double l2 = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            const double x = r0[3 * (int64_t)j + d] - r0[3 * (int64_t)i + d];
+            mx = fmax(mx, fabs(x));
+            l2 += x * x;
+        }
+        mn = fmin(mn, sqrt(l2));
     }
-    for (int off = 16; off >= 1; off >>= 1) mx = fmax(mx, __shfl_xor_sync(kFull, mx, off));
-    if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
+    for (int off = 16; off >= 1; off >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(kFull, mx, off));
+        mn = fmin(mn, __shfl_xor_sync(kFull, mn, off));
+    }
+    if (lane == 0) {
+        atomicMax(out, (unsigned long long)__double_as_longlong(mx));
+        atomicMin(out + 1, (unsigned long long)__double_as_longlong(mn));
+    }
 }
 
 }  // namespace
@@ -554,18 +646,20 @@ int validate_mixed(const pp_fused_args& a) {
     if (a.bond_types && a.nbond_types * a.nregimes > kMaxTable) return PP_ERROR_UNSUPPORTED;
     if (!(a.pos_scale > 0.0)) return PP_ERROR_INVALID_VALUE;
     if (a.variant < 0 || a.variant >= PP_MIXED_VARIANTS) return PP_ERROR_INVALID_VALUE;
+    if (!a.umax || !a.status) return PP_ERROR_INVALID_VALUE;
+    if (a.max_neigh > 256) return PP_ERROR_UNSUPPORTED;
+    if (a.max_neigh >= 64 && !aligned16(a.nlist)) return PP_ERROR_MISALIGNED;  // bulk copies
     return PP_SUCCESS;
 }
 
 int launch_mixed_step(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
     switch (a.max_neigh > 32 ? a.max_neigh / 32 : 1) {
-        case 1: launch_sl<1>(a, parity, l, st); break;
-        case 2: launch_sl<2>(a, parity, l, st); break;
-        case 4: launch_sl<4>(a, parity, l, st); break;
-        case 8: launch_sl<8>(a, parity, l, st); break;
-        default: return PP_ERROR_UNSUPPORTED;  // max_neigh > 256
+        case 1: return launch_sl<1>(a, parity, l, st);
+        case 2: return launch_sl<2>(a, parity, l, st);
+        case 4: return launch_sl<4>(a, parity, l, st);
+        case 8: return launch_sl<8>(a, parity, l, st);
     }
-    return launch_status();
+    return PP_ERROR_UNSUPPORTED;  // max_neigh > 256
 }
 
 }  // namespace pp
@@ -579,7 +673,7 @@ extern "C" int pp_bond_extent(const int32_t* nlist, const double* r0, int32_t nn
     if (!extent) return PP_ERROR_INVALID_VALUE;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     unsigned long long* out = reinterpret_cast<unsigned long long*>(extent);
-    k_zero_u64<<<1, 1, 0, st>>>(out);
+    k_init_extent<<<1, 1, 0, st>>>(out);
     if (nnodes > 0) {
         if (!nlist || !r0) return PP_ERROR_INVALID_VALUE;
         k_bond_extent<<<(nnodes + 7) / 8, 256, 0, st>>>(nlist, r0, nnodes, max_neigh, out);

@@ -378,10 +378,14 @@ class _CUDAIntegrator(Integrator):
         self.sc32_d = (None if self.stiffness_corrections_d is None
                        else self._empty((n, mn), torch.float32))
         self.nflags_d = self._empty((n,), torch.int32)
-        ext = self._zeros((1,), torch.float64)
+        self.umax_d = self._zeros((1,), torch.float32)
+        self.status_d = self._zeros((1,), torch.int32)
+        ext = self._zeros((2,), torch.float64)
         check(lib().pp_bond_extent(_ptr(self.nlist_d), _ptr(self.r0_d), n, mn,
                                    _ptr(ext), self._stream), "pp_bond_extent")
-        self.bond_extent = float(ext.cpu().item())
+        ext = ext.cpu().numpy()
+        self.bond_extent = float(ext[0])
+        self.min_bond = float(ext[1]) if ext[1] < 1e300 else 0.0
         self.pos_origin, self.pos_scale = _pos_frame(self.coords,
                                                      self.bond_extent)
 
@@ -436,6 +440,9 @@ class _CUDAIntegrator(Integrator):
             a.rho32 = _ptr(self.rho32_d)
             a.sc32 = _ptr(self.sc32_d)
             a.nflags = _ptr(self.nflags_d)
+            a.umax = _ptr(self.umax_d)
+            a.status = _ptr(self.status_d)
+            a.min_bond = float(self.min_bond)
             a.pos_scale = float(self.pos_scale)
             for k in range(3):
                 a.pos_origin[k] = float(self.pos_origin[k])
@@ -556,6 +563,12 @@ class _CUDAIntegrator(Integrator):
     def _write(self, u, ud, udd, force, body_force, damage, nlist, n_neigh):
         self._sync_state()
         self.context.stream.synchronize()
+        if self.precision == "mixed":
+            status = int(self.status_d.cpu().item())
+            if status != _lib.PP_STATUS_OK:
+                raise _lib.LibraryError(
+                    f"a mixed-precision step reported status {status}: a bulk "
+                    "copy did not complete and the state is invalid")
         cur = self.u_d[self._parity]
 
         def put(host, dev):

@@ -97,7 +97,7 @@ def test_validation_without_gpu(L):
     base = ctypes.addressof(buf)
     for name in ("r0", "vols", "family", "bc_types", "bc_values",
                  "fc_types", "fc_values", "nlist", "n_neigh", "frc",
-                 "nflags"):
+                 "nflags", "umax", "status"):
         setattr(fa, name, base)
     fa.precision = _lib.PP_MIXED
     fa.pos_q = base + 4
