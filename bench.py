@@ -567,7 +567,7 @@ def main():
                      "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "kernel": "k_fused_mixed",
+                     "kernel": "k_mixed",
                      "kernel_ms": kernel_ms,
                      "peak_source": ("measured" if peaks else "fallback")},
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
