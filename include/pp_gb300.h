@@ -35,6 +35,7 @@ extern "C" {
 #define PP_ERROR_MISALIGNED         3  /* pointer not aligned as required  */
 #define PP_ERROR_UNSUPPORTED        4  /* option combination not built     */
 #define PP_ERROR_CUDA               5  /* a CUDA runtime call failed       */
+#define PP_ERROR_TOO_LARGE          6  /* more steps than the static scratch holds */
 
 /* Integrator kinds (peripy/integrators.py:462, 544, 651). */
 #define PP_EULER                    0
@@ -269,6 +270,48 @@ int pp_mixed_pack(const pp_fused_args* args, int32_t parity, void* stream);
  * (float64) from the PP_MIXED state slot `parity`.  Called by write()
  * (peripy/integrators.py:285-300). */
 int pp_mixed_export(const pp_fused_args* args, int32_t parity, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Fused steps without any device allocation.                               */
+/* ------------------------------------------------------------------------ */
+
+/* Largest nsteps accepted by pp_fused_run_static. */
+#define PP_STATIC_MAX_STEPS         65536
+
+/* No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory themselves -- for instance code running inside a
+ * host runtime whose device memory is pre-reserved and handed out only as
+ * the simulation arrays, or a caller that must not change the device
+ * memory footprint between set-up and the time loop.  pp_fused_run needs a
+ * caller-allocated device copy of the magnitude schedules and a step-index
+ * word, and the mixed-precision step needs two caller-allocated device
+ * words; this entry point needs none of them.
+ *
+ * Same steps as pp_fused_run(args, parity, nsteps, ...) with direct launches
+ * (no CUDA graph), except that disp_mags[k] and force_mags[k] are read from
+ * HOST memory (k = 0..nsteps-1) and copied into a file-scope device array
+ * of the library (1 MB: 2 * PP_STATIC_MAX_STEPS doubles plus two words),
+ * which every GPU that loads the library holds until the process exits.
+ * For PP_MIXED, args->umax and args->status are ignored: the call keeps
+ * those words in the same array, clears the status word and recomputes the
+ * running max |u| from the state at its start; pp_static_status() reads the
+ * status word back.  nsteps > PP_STATIC_MAX_STEPS returns
+ * PP_ERROR_TOO_LARGE.  It calls no cudaMalloc, cudaFree or other allocating
+ * routine.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  All calls share the one array: calls whose
+ * work overlaps on the GPU (different streams, or host threads) race on it
+ * and must be serialised by the caller. */
+int pp_fused_run_static(const pp_fused_args* args, int32_t parity,
+                        int64_t nsteps, const double* disp_mags,
+                        const double* force_mags, void* stream);
+
+/* Copies the status word of the last pp_fused_run_static call on `stream`
+ * (PP_STATUS_*) to *status (host memory) and waits for the stream.  No
+ * counterpart in the reference. */
+int pp_static_status(int32_t* status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,8 @@ PP_ERROR_MAX_NEIGH = 2
 PP_ERROR_MISALIGNED = 3
 PP_ERROR_UNSUPPORTED = 4
 PP_ERROR_CUDA = 5
+PP_ERROR_TOO_LARGE = 6
+PP_STATIC_MAX_STEPS = 65536
 
 PP_EULER = 0
 PP_EULER_CROMER = 1
@@ -102,6 +104,9 @@ SIGNATURES = {
     "pp_bond_extent": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
     "pp_mixed_pack": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
     "pp_mixed_export": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
+    "pp_fused_run_static": (
+        ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _i64, _vp, _vp, _vp]),
+    "pp_static_status": (ctypes.c_int, [_vp, _vp]),
 }
 
 _lock = threading.Lock()

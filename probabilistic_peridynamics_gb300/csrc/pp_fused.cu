@@ -88,7 +88,9 @@ __global__ void __launch_bounds__(256) k_fused_f64(pp_fused_args a, int parity, 
 __global__ void k_set_base(int64_t* base, int64_t v) { *base = v; }
 __global__ void k_advance_base(int64_t* base, int64_t by) { *base += by; }
 
-int validate(const pp_fused_args& a) {
+}  // namespace
+
+int validate_fused(const pp_fused_args& a) {
     if (a.nnodes < 0) return PP_ERROR_INVALID_VALUE;
     if (!is_pow2_le_1024(a.max_neigh)) return PP_ERROR_MAX_NEIGH;
     if (a.integrator < PP_EULER || a.integrator > PP_VELOCITY_VERLET) return PP_ERROR_INVALID_VALUE;
@@ -112,6 +114,8 @@ int validate(const pp_fused_args& a) {
     return PP_ERROR_INVALID_VALUE;
 }
 
+namespace {
+
 template <int SL, bool CORR, bool TYPES>
 void launch_f64_variant(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
     const int wpb = a.nodes_per_block > 0 ? a.nodes_per_block : kDefaultWarps;
@@ -129,7 +133,9 @@ void launch_f64_sl(const pp_fused_args& a, int parity, const Launch& l, cudaStre
     if (corr && types) launch_f64_variant<SL, true, true>(a, parity, l, st);
 }
 
-int launch_step(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
+}  // namespace
+
+int launch_fused_step(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
     if (a.precision == PP_MIXED) return launch_mixed_step(a, parity, l, st);
     switch (a.max_neigh > 32 ? a.max_neigh / 32 : 1) {
         case 1: launch_f64_sl<1>(a, parity, l, st); break;
@@ -143,7 +149,6 @@ int launch_step(const pp_fused_args& a, int parity, const Launch& l, cudaStream_
     return launch_status();
 }
 
-}  // namespace
 }  // namespace pp
 
 using namespace pp;
@@ -152,10 +157,10 @@ extern "C" int pp_fused_step(const pp_fused_args* args, int32_t parity,
                              double displacement_bc_magnitude, double force_bc_magnitude,
                              void* stream) {
     if (!args || (parity != 0 && parity != 1)) return PP_ERROR_INVALID_VALUE;
-    const int v = validate(*args);
+    const int v = validate_fused(*args);
     if (v != PP_SUCCESS || args->nnodes == 0) return v;
     const Launch l{displacement_bc_magnitude, force_bc_magnitude, nullptr, nullptr, nullptr, 0};
-    return launch_step(*args, parity, l, static_cast<cudaStream_t>(stream));
+    return launch_fused_step(*args, parity, l, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t nsteps,
@@ -165,7 +170,7 @@ extern "C" int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t n
     if (!args || (parity != 0 && parity != 1) || nsteps < 0 || first < 0)
         return PP_ERROR_INVALID_VALUE;
     if (!disp_mags || !force_mags) return PP_ERROR_INVALID_VALUE;
-    const int v = validate(*args);
+    const int v = validate_fused(*args);
     if (v != PP_SUCCESS || args->nnodes == 0 || nsteps == 0) return v;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int64_t done = 0;
@@ -183,7 +188,7 @@ extern "C" int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t n
         int rc = PP_SUCCESS;
         for (int k = 0; k < chunk && rc == PP_SUCCESS; ++k) {
             const Launch l{0.0, 0.0, disp_mags, force_mags, step_base, k};
-            rc = launch_step(*args, p ^ (k & 1), l, st);
+            rc = launch_fused_step(*args, p ^ (k & 1), l, st);
         }
         if (rc == PP_SUCCESS) {
             k_advance_base<<<1, 1, 0, st>>>(step_base, chunk);
@@ -208,7 +213,7 @@ extern "C" int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t n
     }
     for (int64_t k = done; k < nsteps; ++k) {
         const Launch l{0.0, 0.0, disp_mags, force_mags, nullptr, first + k};
-        const int rc = launch_step(*args, p, l, st);
+        const int rc = launch_fused_step(*args, p, l, st);
         if (rc != PP_SUCCESS) return rc;
         p ^= 1;
     }

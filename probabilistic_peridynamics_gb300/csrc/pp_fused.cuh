@@ -32,4 +32,10 @@ int launch_mixed_step(const pp_fused_args& a, int parity, const Launch& l, cudaS
 // Checks of the PP_MIXED arguments beyond the common ones (pp_mixed.cu).
 int validate_mixed(const pp_fused_args& a);
 
+// All argument checks of a fused step (pp_fused.cu).
+int validate_fused(const pp_fused_args& a);
+
+// Launches one fused step of either precision (pp_fused.cu).
+int launch_fused_step(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st);
+
 }  // namespace pp

@@ -210,6 +210,7 @@ extern "C" const char* pp_status_string(int status) {
         case PP_ERROR_MISALIGNED: return "pointer not 16-byte aligned";
         case PP_ERROR_UNSUPPORTED: return "unsupported option combination";
         case PP_ERROR_CUDA: return "CUDA runtime error";
+        case PP_ERROR_TOO_LARGE: return "nsteps exceeds PP_STATIC_MAX_STEPS";
     }
     return "unknown status";
 }
