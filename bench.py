@@ -82,6 +82,11 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--accuracy-steps", type=int, default=E2E_STEPS)
+    p.add_argument("--workload", choices=["large", "batched"],
+                   default="large",
+                   help="large: the 200x200x10 Velocity-Verlet plate (the "
+                        "headline); batched: 64 uneven UQ instances, "
+                        "Euler-Cromer")
     p.add_argument("--profile", choices=["mixed", "fp64", "plain"],
                    help="only run 3 warm-up and 3 profiled launches of one "
                         "step variant on the full workload (for ncu)")
@@ -474,6 +479,47 @@ def load_traffic():
     return None
 
 
+def batched_main(args):
+    """64 uneven UQ instances in one persistent launch per step."""
+    import torch
+    import probabilistic_peridynamics_gb300 as pp
+    from probabilistic_peridynamics_gb300 import batch, lattice
+    t0 = time.perf_counter()
+    inst = batch.uq_instances(count=64, seed=2024, dx=DX)
+    b = batch.concatenate(inst)
+    setup_s = time.perf_counter() - t0
+    k = lattice.bond_stiffness_pmb(BULK_MODULUS, HORIZON_CELLS * DX)
+    integ = pp.EulerCromerCUDA(DAMPING, dt=DT, precision="mixed")
+    sim = batch.BatchedSimulation(b, integ, k)
+    steps, warmup = args.steps, args.warmup
+    ms = time_steps(integ, steps, warmup, torch)
+    value = b.bonds * steps / (ms * 1e-3)
+    kernel_ms = time_kernel_launches(integ, 50, torch)
+    alg = b.bonds * (4 + 8) + b.nnodes * B_NODE_VV
+    peaks = load_peaks()
+    peak = float(peaks["hbm_gbs"]) if peaks else 6800.0
+    achieved = alg / (kernel_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched UQ: 64 instances nx,ny~U{60..200}, "
+                               "nz=5, Euler-Cromer, lognormal s0, "
+                               "U(0.9,1.1) bond noise",
+                   "nodes": b.nnodes, "bonds": b.bonds,
+                   "instances": len(inst), "setup_s": setup_s,
+                   "tile_shape_autotune_ms": integ.tuning,
+                   "variant": int(integ._fargs.variant)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "algorithmic_bytes_per_launch": alg,
+                     "kernel_ms": kernel_ms},
+        "gpu_launches": steps + (steps // 16 + 1 if steps >= 32 else 0),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.profile:
@@ -481,6 +527,9 @@ def main():
         return
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.workload == "batched":
+        batched_main(args)
         return
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))

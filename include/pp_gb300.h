@@ -48,7 +48,7 @@ extern "C" {
                                           double-float node state          */
 
 /* Number of PP_MIXED kernel variants (pp_fused_args.variant). */
-#define PP_MIXED_VARIANTS           2
+#define PP_MIXED_VARIANTS           3
 
 /* Values of pp_fused_args.status after a step (read by the caller). */
 #define PP_STATUS_OK                0
@@ -183,9 +183,11 @@ typedef struct pp_fused_args {
     int32_t nbond_types;
     int32_t flags;
     int32_t nodes_per_block;       /* PP_FLOAT64: warps per block (0 = 8)  */
-    int32_t variant;               /* PP_MIXED kernel variant, 0..PP_MIXED_VARIANTS-1:
-                                      register budget for 2 (0) or 3 (1)
-                                      resident CTAs per SM               */
+    int32_t variant;               /* PP_MIXED tile shape, 0..PP_MIXED_VARIANTS-1:
+                                      0: 8 warps x 64 nodes per CTA, register
+                                      budget for 2 resident CTAs per SM;
+                                      1: 8 warps x 64 nodes, 3 CTAs/SM;
+                                      2: 4 warps x 32 nodes, 6 CTAs/SM   */
     int32_t reserved;              /* must be 0                            */
     double dt;
     double damping;
@@ -205,6 +207,12 @@ typedef struct pp_fused_args {
     const double* densities;       /* EC / VV                              */
     const double* stiffness_corrections;  /* or NULL                       */
     const int32_t* bond_types;     /* or NULL                              */
+    /* batched independent instances (PMB only): node i uses critical
+       stretch instance_s0[node_instance[i]]; NULL = one model          */
+    const int32_t* node_instance;  /* (nnodes) or NULL                     */
+    const double* instance_s0;     /* (ninstances)                         */
+    int32_t ninstances;            /* 1..256 when node_instance != NULL    */
+    int32_t reserved2;             /* must be 0                            */
     /* mutable bond state */
     int32_t* nlist;
     int32_t* regimes;              /* with bond_types                      */

@@ -29,7 +29,7 @@ PP_FLOAT64 = 0
 PP_MIXED = 1
 
 PP_FLAG_COMPENSATED = 1
-PP_MIXED_VARIANTS = 2
+PP_MIXED_VARIANTS = 3
 PP_STATUS_OK = 0
 PP_STATUS_COPY_TIMEOUT = 1
 
@@ -70,7 +70,8 @@ class FusedArgs(ctypes.Structure):
         ("r0", _vp), ("vols", _vp), ("family", _vp), ("bc_types", _vp),
         ("bc_values", _vp), ("fc_types", _vp), ("fc_values", _vp),
         ("densities", _vp), ("stiffness_corrections", _vp),
-        ("bond_types", _vp),
+        ("bond_types", _vp), ("node_instance", _vp), ("instance_s0", _vp),
+        ("ninstances", _i32), ("reserved2", _i32),
         ("nlist", _vp), ("regimes", _vp),
         ("u", _vp * 2), ("ud", _vp), ("udd", _vp), ("force", _vp),
         ("body_force", _vp), ("n_neigh", _vp), ("damage", _vp),

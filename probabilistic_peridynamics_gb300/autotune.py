@@ -43,7 +43,8 @@ def tune_mixed(integ, warmup=3, reps=10):
     import torch
     fa = integ._fargs
     key = ("mixed", fa.nnodes, fa.max_neigh, fa.integrator,
-           bool(fa.stiffness_corrections), bool(fa.bond_types), fa.flags)
+           bool(fa.stiffness_corrections), bool(fa.bond_types),
+           bool(fa.node_instance), fa.flags)
     if key in _cache:
         fa.variant = _cache[key][0]
         return _cache[key][1]

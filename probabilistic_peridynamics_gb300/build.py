@@ -25,8 +25,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE)]
 #: Per-unit flags.  The mixed-precision step accepts flushed denormals and
 #: approximate FP32 division/square root: its error band covers them.
-UNIT_FLAGS = {"pp_mixed.cu": ["-ftz=true", "-prec-div=false",
-                              "-prec-sqrt=false"]}
+UNIT_FLAGS = {"pp_mixed": ["-ftz=true", "-prec-div=false",
+                           "-prec-sqrt=false"]}
 
 
 def _nvcc():
@@ -62,8 +62,9 @@ def build(force=False, verbose=False):
 
     def compile_one(job):
         src, obj = job
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *UNIT_FLAGS.get(src.name, []), "-c",
-               str(src), "-o", str(obj)]
+        extra = [f for prefix, flags in UNIT_FLAGS.items()
+                 if src.name.startswith(prefix) for f in flags]
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
         res = subprocess.run(cmd, capture_output=True, text=True)

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(256) k_fused_f64(pp_fused_args a, int parity, 
                     a.critical_stretch_table,
                     a.plus_cs,
                     a.bond_stiffness,
-                    a.critical_stretch,
+                    a.node_instance ? a.instance_s0[a.node_instance[i]] : a.critical_stretch,
                     a.nregimes};
     const int64_t o3 = 3 * (int64_t)i;
     const d3 ri{a.r0[o3], a.r0[o3 + 1], a.r0[o3 + 2]};
@@ -95,7 +95,10 @@ int validate_fused(const pp_fused_args& a) {
     if (!is_pow2_le_1024(a.max_neigh)) return PP_ERROR_MAX_NEIGH;
     if (a.integrator < PP_EULER || a.integrator > PP_VELOCITY_VERLET) return PP_ERROR_INVALID_VALUE;
     if (a.nodes_per_block < 0 || a.nodes_per_block > 32) return PP_ERROR_INVALID_VALUE;
-    if (a.reserved != 0) return PP_ERROR_INVALID_VALUE;
+    if (a.reserved != 0 || a.reserved2 != 0) return PP_ERROR_INVALID_VALUE;
+    if (a.node_instance &&
+        (a.bond_types || !a.instance_s0 || a.ninstances < 1 || a.ninstances > 256))
+        return PP_ERROR_INVALID_VALUE;
     if (a.nnodes == 0) return PP_SUCCESS;
     if (!a.r0 || !a.vols || !a.family || !a.bc_types || !a.bc_values || !a.fc_types ||
         !a.fc_values || !a.nlist || !a.n_neigh)

@@ -1,538 +1,11 @@
-// pp_mixed.cu -- PP_MIXED fused step: FP32 bond arithmetic on compact
-// gathers, the break / regime decision taken exactly as binary64 would on
-// the same state, and double-float node state.
-//
-// Structure of one launch (one CTA = 8 warps = 64 consecutive nodes):
-//
-//  1. Bond phase, one warp per node (8 nodes per warp, the CTA's warps
-//     working on 8 consecutive nodes at a time so their neighbourhoods share
-//     L1 lines).  For the lane's max_neigh/32 slots: load all neighbour
-//     indices, then all gathers (int4 fixed-point position + k*vol, float4
-//     displacement + max|u|), then the FP32 bond arithmetic.  A slot whose
-//     FP32 stretch lies within the proven error band of a critical stretch
-//     is deferred to a slow path that evaluates the binary64 stretch of
-//     peridynamics.cl:65-75 from the reference r0 and the exact
-//     double-float displacement.  The four per-node sums (force x, y, z and
-//     the intact count) are reduced with a 6-shuffle transposed butterfly
-//     and parked in shared memory.
-//  2. Node phase, all 256 threads: thread (node, component) applies the
-//     force boundary condition and the integrator update of one DOF in
-//     double-float arithmetic; every load and store of the node state is a
-//     contiguous 1 KB access per CTA.
-//
-// Integer-to-float conversion uses the exponent trick
-// float(q) = bits(0x4B400000 + q) - 1.5*2^23 (exact for |q| < 2^22), folded
-// with the fixed-point scale into one FMA: on GB300 the I2F instruction
-// runs on the FP64 pipe, which would otherwise bound this kernel.
-//
-// This translation unit is compiled with -ftz=true -prec-div=false
-// -prec-sqrt=false: every FP32 rounding and approximation is covered by the
-// error band; the double-float operations use explicit _rn intrinsics and
-// the binary64 slow path is unaffected by those flags.
-#include "pp_bond_f64.cuh"
-#include "pp_fused.cuh"
-#include "pp_tma.cuh"
+// pp_mixed.cu -- PP_MIXED set-up (pack, export, bond extent), argument
+// checks and dispatch of a step to its tile shape.  The kernel itself is in
+// pp_mixed.cuh, instantiated per tile shape in pp_mixed_v*.cu.
+#include "pp_mixed.cuh"
 
 namespace pp {
+namespace mixed {
 namespace {
-
-constexpr int kWarps = 8;
-constexpr int kChunk = 64;  // nodes per CTA
-constexpr int kMaxTable = 256;
-
-constexpr int kMagicI = 0x4B400000;  // bit pattern of 1.5 * 2^23
-constexpr float kMagicF = 12582912.0f;
-
-struct MixedConst {
-    float h;        // fixed-point step (a power of two)
-    float mh;       // -kMagicF * h
-    float geo;      // sqrt(3) * h: bound on the rounding of each xi
-    float rxi_max;  // 1 / (smallest bond length)
-    float s0;       // critical stretch (PMB), rounded to float
-    float s0_err;   // 6e-8 * |s0|: rounding of s0 to float
-    float dt_hi, dt_lo;
-    float half_hi, half_lo;
-    float damping;
-};
-
-// FP32 quantities of one bond (i -> j).
-struct Bond32 {
-    float px, py, pz;  // deformed bond vector
-    float s;           // stretch
-    float ry;          // 1 / |p|
-    float rxi;         // 1 / |xi|
-};
-
-__device__ __forceinline__ float fixed_diff(int qj, int qi, const MixedConst& c) {
-    return fmaf(__int_as_float(qj - qi + kMagicI), c.h, c.mh);
-}
-
-__device__ __forceinline__ Bond32 bond32(const int4& qi, const float4& ui, const int4& qj,
-                                         const float4& uj, const MixedConst& c) {
-    const float xx = fixed_diff(qj.x, qi.x, c);
-    const float xy = fixed_diff(qj.y, qi.y, c);
-    const float xz = fixed_diff(qj.z, qi.z, c);
-    const float ex = uj.x - ui.x, ey = uj.y - ui.y, ez = uj.z - ui.z;
-    Bond32 b;
-    b.px = xx + ex;
-    b.py = xy + ey;
-    b.pz = xz + ez;
-    const float mx = b.px + xx, my = b.py + xy, mz = b.pz + xz;  // 2 xi + e
-    const float xi2 = fmaf(xx, xx, fmaf(xy, xy, xz * xz));
-    const float y2 = fmaf(b.px, b.px, fmaf(b.py, b.py, b.pz * b.pz));
-    const float num = fmaf(ex, mx, fmaf(ey, my, ez * mz));  // |p|^2 - |xi|^2
-    b.rxi = rsqrtf(xi2);
-    b.ry = rsqrtf(y2);
-    const float lsum = fmaf(y2, b.ry, xi2 * b.rxi);  // |p| + |xi|
-    // s = (|p| - |xi|)/|xi| without cancellation: (2 xi.e + e.e)/(|xi|(|p|+|xi|))
-    b.s = __fdividef(num * b.rxi, lsum);
-    return b;
-}
-
-// Bound on |s - s64| for one bond: s64 is the binary64 stretch of the same
-// state (reference formula).  Terms: geometry (fixed-point rounding of xi,
-// <= sqrt(3) h per bond vector), the rounding of the displacement to float
-// (<= 2^-24 |u| per component), FP32 arithmetic (<= 1e-6 relative, which
-// covers the approximate rsqrt and division), times a safety factor 2.
-__device__ __forceinline__ float band32(const float4& ui, const float4& uj, const Bond32& b,
-                                        const MixedConst& c) {
-    const float einf =
-        fmaxf(fabsf(uj.x - ui.x), fmaxf(fabsf(uj.y - ui.y), fabsf(uj.z - ui.z)));
-    const float r = 1.7320508f * einf * b.rxi;  // >= |e| / |xi|
-    const float t2 = fmaf(2.0f, r, fabsf(b.s));
-    const float geo = fmaf(c.geo, b.rxi, 1.1e-7f);
-    const float uterm = 1.1e-7f * (ui.w + uj.w + einf) * b.rxi;
-    const float arith = 1.0e-6f * fmaf(r, r, t2);
-    return fmaf(2.0f, fmaf(geo, t2, uterm + arith), 1.0e-12f);
-}
-
-// A bound of band32 valid for every bond of the step, affine in |s|:
-// band32 <= quick_a + quick_c * |s|, from the running max |u| (U) and the
-// shortest bond.  Decides almost every bond with three instructions.
-struct QuickBand {
-    float a, c;
-};
-
-__device__ __forceinline__ QuickBand quick_band(float U, const MixedConst& c) {
-    const float geo = fmaf(c.geo, c.rxi_max, 1.1e-7f);
-    const float R = 3.5f * U * c.rxi_max;  // >= sqrt(3) * (|u_i| + |u_j|)(1 + eps) / |xi|
-    QuickBand q;
-    q.a = 2.0f * (geo * 2.0f * R + 1.1e-7f * 4.1f * U * c.rxi_max +
-                  1.0e-6f * fmaf(R, R, 2.0f * R)) +
-          1.0e-12f;
-    q.c = 2.0f * (geo + 1.0e-6f);
-    return q;
-}
-
-// Binary64 stretch of bond (i, j) from the reference r0 and the exact
-// double-float displacement, in the reference operation order
-// (peridynamics.cl:65-75).
-__device__ __noinline__ double exact_stretch(const pp_fused_args& a, int parity, int i, int j) {
-    const float4 hi_i = ldg_f4(a.uhi[parity], i), lo_i = ldg_f4(a.ulo[parity], i);
-    const float4 hi_j = ldg_f4(a.uhi[parity], j), lo_j = ldg_f4(a.ulo[parity], j);
-    const double* ri = a.r0 + 3 * (int64_t)i;
-    const double* rj = a.r0 + 3 * (int64_t)j;
-    const double uix = dadd((double)hi_i.x, (double)lo_i.x);
-    const double uiy = dadd((double)hi_i.y, (double)lo_i.y);
-    const double uiz = dadd((double)hi_i.z, (double)lo_i.z);
-    const double ujx = dadd((double)hi_j.x, (double)lo_j.x);
-    const double ujy = dadd((double)hi_j.y, (double)lo_j.y);
-    const double ujz = dadd((double)hi_j.z, (double)lo_j.z);
-    const double xi_x = dsub(rj[0], ri[0]);
-    const double xi_y = dsub(rj[1], ri[1]);
-    const double xi_z = dsub(rj[2], ri[2]);
-    const double xe_x = dadd(dsub(ujx, uix), xi_x);
-    const double xe_y = dadd(dsub(ujy, uiy), xi_y);
-    const double xe_z = dadd(dsub(ujz, uiz), xi_z);
-    const double xi = dsqrt(dadd(dadd(dmul(xi_x, xi_x), dmul(xi_y, xi_y)), dmul(xi_z, xi_z)));
-    const double y = dsqrt(dadd(dadd(dmul(xe_x, xe_x), dmul(xe_y, xe_y)), dmul(xe_z, xe_z)));
-    return ddiv(dsub(y, xi), xi);
-}
-
-// Regime logic of bond_force3/4 (peridynamics.cl:345-367) on a decision
-// function lt(threshold index) = (s < critical_stretch[idx]).
-// Returns the new regime (>= nregimes means broken).
-template <class Lt>
-__device__ __forceinline__ int next_regime(int reg, int base, int nr, Lt&& lt) {
-    const int rc = reg < 0 ? 0 : (reg >= nr ? nr - 1 : reg);
-    if (lt(base + rc)) {
-        if (reg > 0 && rc > 0 && lt(base + rc - 1)) return reg - 1;
-        return reg;
-    }
-    return reg + 1;
-}
-
-// Sum (x, y, z, w) over the warp: 6 shuffles.  Lanes 0-7 end with the x
-// total, 8-15 y, 16-23 z, 24-31 w.
-__device__ __forceinline__ float reduce4(float x, float y, float z, float w, int lane) {
-    const bool up16 = lane & 16;
-    const float a_keep = up16 ? z : x, a_send = up16 ? x : z;
-    const float b_keep = up16 ? w : y, b_send = up16 ? y : w;
-    const float a = a_keep + __shfl_xor_sync(kFull, a_send, 16);
-    const float b = b_keep + __shfl_xor_sync(kFull, b_send, 16);
-    const bool up8 = lane & 8;
-    float v = (up8 ? b : a) + __shfl_xor_sync(kFull, up8 ? a : b, 8);
-    v += __shfl_xor_sync(kFull, v, 4);
-    v += __shfl_xor_sync(kFull, v, 2);
-    v += __shfl_xor_sync(kFull, v, 1);
-    return v;
-}
-
-constexpr uint32_t kWaitPolls = 1u << 22;  // bound on mbarrier polls
-
-struct alignas(16) MixedShared {
-    uint64_t bar[2];
-    float4 frc[kChunk];
-    float thr[kMaxTable], k[kMaxTable], c[kMaxTable];
-};
-
-// Bond phase of one node (one warp): returns nothing, parks the reduced
-// (force x, y, z, intact count) of local node li in sh.frc[li].
-template <int SL, bool CORR, bool TYPES>
-__device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const MixedConst& c,
-                                                const QuickBand& qb, MixedShared& sh,
-                                                const int32_t* nl_row, int parity, int i,
-                                                int li, int lane) {
-    const int L = a.max_neigh;
-    const int nr = a.nregimes;
-    const int64_t row = (int64_t)i * L;
-    const float* __restrict__ uhi = a.uhi[parity];
-    const int4 qi = ldg_i4(a.pos_q, i);
-    const float4 ui = ldg_f4(uhi, i);
-    int jr[SL];
-#pragma unroll
-    for (int k = 0; k < SL; ++k) {
-        const int slot = lane + 32 * k;
-        jr[k] = (SL > 1 || slot < L) ? nl_row[slot] : -1;
-    }
-    int4 qj[SL];
-    float4 uj[SL];
-    float sc[SL];
-    int bt[SL], rg[SL];
-#pragma unroll
-    for (int k = 0; k < SL; ++k) {
-        // An empty slot gets a harmless stand-in (one fixed-point step away,
-        // same displacement) so that all arithmetic stays finite.
-        if (jr[k] != -1) {
-            qj[k] = ldg_i4(a.pos_q, jr[k]);
-            uj[k] = ldg_f4(uhi, jr[k]);
-        } else {
-            qj[k] = make_int4(qi.x + 1, qi.y, qi.z, 0);
-            uj[k] = ui;
-        }
-        const int64_t gid = row + lane + 32 * k;
-        if constexpr (CORR) sc[k] = jr[k] != -1 ? __ldcs(a.sc32 + gid) : 0.f;
-        if constexpr (TYPES) {
-            bt[k] = jr[k] != -1 ? __ldcs(a.bond_types + gid) * nr : 0;
-            rg[k] = jr[k] != -1 ? a.regimes[gid] : 0;
-        }
-    }
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    float cnt = 0.f;
-    unsigned amb = 0u;
-#pragma unroll
-    for (int k = 0; k < SL; ++k) {
-        if (jr[k] == -1) continue;
-        const int64_t gid = row + lane + 32 * k;
-        const Bond32 b = bond32(qi, ui, qj[k], uj[k], c);
-        const float quick = fmaf(qb.c, fabsf(b.s), qb.a);
-        float w = __int_as_float(qj[k].w);  // k*vol (PMB) or vol (types)
-        bool intact;
-        if constexpr (!TYPES) {
-            const float d = b.s - c.s0;
-            if (!(fabsf(d) > quick)) {
-                if (!(fabsf(d) > band32(ui, uj[k], b, c) + c.s0_err)) {
-                    amb |= 1u << k;
-                    continue;
-                }
-            }
-            intact = d < 0.0f;
-            w *= b.s;
-        } else {
-            bool ambiguous = false;
-            const int reg = next_regime(rg[k], bt[k], nr, [&](int idx) {
-                const float thr = sh.thr[idx];
-                const float d = b.s - thr;
-                const float err = 6.0e-8f * fabsf(thr);
-                if (!(fabsf(d) > quick + err) &&
-                    !(fabsf(d) > band32(ui, uj[k], b, c) + err))
-                    ambiguous = true;
-                return d < 0.0f;
-            });
-            if (ambiguous) {
-                amb |= 1u << k;
-                continue;
-            }
-            if (reg != rg[k]) a.regimes[gid] = reg;
-            intact = reg < nr;
-            if (intact) w *= fmaf(b.s, sh.k[bt[k] + reg], sh.c[bt[k] + reg]);
-        }
-        if (!intact) {
-            a.nlist[gid] = -1;
-            continue;
-        }
-        float fv = w * b.ry;
-        if constexpr (CORR) fv *= sc[k];
-        sx = fmaf(fv, b.px, sx);
-        sy = fmaf(fv, b.py, sy);
-        sz = fmaf(fv, b.pz, sz);
-        cnt += 1.0f;
-    }
-    // Slow path: slots whose FP32 stretch is too close to a critical stretch
-    // are decided on the binary64 stretch.
-    if (__any_sync(kFull, amb != 0u)) {
-#pragma unroll
-        for (int k = 0; k < SL; ++k) {
-            if (!((amb >> k) & 1u)) continue;
-            const int64_t gid = row + lane + 32 * k;
-            const Bond32 b = bond32(qi, ui, qj[k], uj[k], c);
-            const double s64 = exact_stretch(a, parity, i, jr[k]);
-            float w = __int_as_float(qj[k].w);
-            bool intact;
-            if constexpr (!TYPES) {
-                intact = s64 < a.critical_stretch;
-                w *= b.s;
-            } else {
-                const int reg = next_regime(rg[k], bt[k], nr, [&](int idx) {
-                    return s64 < a.critical_stretch_table[idx];
-                });
-                if (reg != rg[k]) a.regimes[gid] = reg;
-                intact = reg < nr;
-                if (intact) w *= fmaf(b.s, sh.k[bt[k] + reg], sh.c[bt[k] + reg]);
-            }
-            if (!intact) {
-                a.nlist[gid] = -1;
-                continue;
-            }
-            float fv = w * b.ry;
-            if constexpr (CORR) fv *= sc[k];
-            sx = fmaf(fv, b.px, sx);
-            sy = fmaf(fv, b.py, sy);
-            sz = fmaf(fv, b.pz, sz);
-            cnt += 1.0f;
-        }
-    }
-    const float v = reduce4(sx, sy, sz, cnt, lane);
-    if ((lane & 7) == 0) reinterpret_cast<float*>(&sh.frc[li])[lane >> 3] = v;
-}
-
-// Node phase of one chunk: thread (node, component) updates one DOF.
-__device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedConst& c,
-                                           const MixedShared& sh, const StepMags& m,
-                                           int parity, int node0) {
-    const int li = threadIdx.x >> 2;
-    const int comp = threadIdx.x & 3;
-    const int i = node0 + li;
-    const bool active = i < a.nnodes;
-    const float4 fr = sh.frc[li];
-    const int64_t o4 = 4 * (int64_t)i + comp;
-    float hi_new = 0.f, lo_new = 0.f;
-    if (active && comp < 3) {
-        const float body = comp == 0 ? fr.x : (comp == 1 ? fr.y : fr.z);
-        const int fl = a.nflags[i];
-        const int64_t o3 = 3 * (int64_t)i + comp;
-        float frc = body;
-        if ((fl >> (3 + comp)) & 1) frc = (float)((double)body + m.force * a.fc_values[o3]);
-        df uu{a.uhi[parity][o4], a.ulo[parity][o4]};
-        const df dt{c.dt_hi, c.dt_lo};
-        if (a.integrator == PP_EULER) {
-            uu = df_add(uu, df_mul_f(dt, frc));
-        } else {
-            const df half{c.half_hi, c.half_lo};
-            const int64_t o8 = 8 * (int64_t)i + comp;
-            df v{a.vel[o8], a.vel[o8 + 4]};
-            const float rho = a.rho32[o4];
-            float acc;
-            if (a.integrator == PP_EULER_CROMER) {
-                acc = __fdiv_rn(frc - c.damping * v.hi, rho);
-                v = df_add(v, df_mul_f(dt, acc));
-                uu = df_add(uu, df_mul(dt, v));
-            } else {
-                const df v1 = df_add(v, df_mul_f(half, a.acc[o4]));
-                acc = __fdiv_rn(frc - c.damping * v1.hi, rho);
-                v = df_add(v1, df_mul_f(half, acc));
-                uu = df_add(uu, df_mul(dt, df_add(v, df_mul_f(half, acc))));
-            }
-            a.vel[o8] = v.hi;
-            a.vel[o8 + 4] = v.lo;
-            a.acc[o4] = acc;
-        }
-        if (fl & (1 << comp)) uu = df_from_double(m.disp * a.bc_values[o3]);
-        hi_new = uu.hi;
-        lo_new = uu.lo;
-        a.frc[8 * (int64_t)i + comp] = frc;
-        a.frc[8 * (int64_t)i + 4 + comp] = body;
-    }
-    // max |u| of the node (quad shuffle) for the next step's error bounds
-    float um = fabsf(hi_new);
-    um = fmaxf(um, __shfl_xor_sync(kFull, um, 1));
-    um = fmaxf(um, __shfl_xor_sync(kFull, um, 2));
-    um *= 1.0f + 1.2e-7f;
-    if (active) {
-        if (comp < 3) {
-            a.uhi[parity ^ 1][o4] = hi_new;
-            a.ulo[parity ^ 1][o4] = lo_new;
-        } else {
-            a.uhi[parity ^ 1][o4] = um;
-            a.ulo[parity ^ 1][o4] = 0.f;
-            a.n_neigh[i] = (int)fr.w;
-        }
-    }
-    // running max |u| over the whole model (non-negative floats order as ints)
-    const int wmax = __reduce_max_sync(kFull, active ? __float_as_int(um) : 0);
-    if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(reinterpret_cast<int*>(a.umax), wmax);
-}
-
-// One CTA loops over chunks of kChunk nodes.  For SL >= 2 the chunk's
-// neighbour-list rows (contiguous) stream into shared memory by bulk copy,
-// double-buffered one chunk ahead; for SL == 1 they are read in place.
-template <int SL, bool CORR, bool TYPES, int MINB>
-__global__ void __launch_bounds__(kWarps * 32, MINB)
-    k_mixed(pp_fused_args a, MixedConst c, int parity, Launch l) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    MixedShared& sh = *reinterpret_cast<MixedShared*>(smem_raw);
-    int32_t* s_nl = reinterpret_cast<int32_t*>(smem_raw + sizeof(MixedShared));
-    constexpr bool kBulk = SL >= 2;
-    const int L = a.max_neigh;
-    const int nchunks = (a.nnodes + kChunk - 1) / kChunk;
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    if constexpr (TYPES) {
-        const int nt = a.nbond_types * a.nregimes;
-        for (int t = threadIdx.x; t < nt; t += blockDim.x) {
-            sh.thr[t] = (float)a.critical_stretch_table[t];
-            sh.k[t] = (float)a.bond_stiffness_table[t];
-            sh.c[t] = (float)a.plus_cs[t];
-        }
-    }
-    uint64_t policy = 0;
-    auto issue = [&](int chunk, int buf) {
-        const int n0 = chunk * kChunk;
-        const int nn = min(kChunk, a.nnodes - n0);
-        const uint32_t bytes = (uint32_t)nn * (uint32_t)L * 4u;
-        mbar_arrive_expect_tx(&sh.bar[buf], bytes);
-        bulk_copy_g2s(s_nl + (size_t)buf * kChunk * L, a.nlist + (int64_t)n0 * L, bytes,
-                      &sh.bar[buf], policy);
-    };
-    if constexpr (kBulk) {
-        if (threadIdx.x == 0) {
-            policy = l2_evict_first_policy();
-            mbar_init(&sh.bar[0], 1);
-            mbar_init(&sh.bar[1], 1);
-            fence_mbar_init();
-        }
-        __syncthreads();
-        if (threadIdx.x == 0 && (int)blockIdx.x < nchunks) issue(blockIdx.x, 0);
-    } else {
-        __syncthreads();
-    }
-    const StepMags m = step_mags(l);
-    const float U = __ldcg(a.umax);
-    const QuickBand qb = quick_band(U, c);
-    int it = 0;
-    for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x, ++it) {
-        const int buf = it & 1;
-        const int node0 = chunk * kChunk;
-        if constexpr (kBulk) {
-            const int next = chunk + gridDim.x;
-            if (threadIdx.x == 0 && next < nchunks) issue(next, buf ^ 1);
-            const bool ok = mbar_wait_bounded(&sh.bar[buf], (it >> 1) & 1, kWaitPolls);
-            if (__syncthreads_or(!ok)) {
-                // A copy never completed: report, drain the other buffer's
-                // copy (bounded), and leave without touching the state.
-                if (threadIdx.x == 0) {
-                    atomicExch(a.status, PP_STATUS_COPY_TIMEOUT);
-                    if (next < nchunks)
-                        mbar_wait_bounded(&sh.bar[buf ^ 1], ((it + 1) >> 1) & 1, kWaitPolls);
-                }
-                return;
-            }
-        }
-        for (int t = 0; t < kChunk / kWarps; ++t) {
-            const int li = t * kWarps + warp;
-            const int i = node0 + li;
-            if (i >= a.nnodes) break;  // warp-uniform
-            const int32_t* nl_row = kBulk ? s_nl + (size_t)buf * kChunk * L + (size_t)li * L
-                                          : a.nlist + (int64_t)i * L;
-            bond_phase_node<SL, CORR, TYPES>(a, c, qb, sh, nl_row, parity, i, li, lane);
-        }
-        __syncthreads();
-        node_phase(a, c, sh, m, parity, node0);
-        __syncthreads();
-    }
-}
-
-MixedConst mixed_const(const pp_fused_args& a) {
-    MixedConst c;
-    c.h = (float)a.pos_scale;
-    c.mh = -kMagicF * c.h;
-    c.geo = 1.7320508f * c.h;
-    c.rxi_max = a.min_bond > 0.0 ? (float)(1.0 / a.min_bond) : 3.0e38f;
-    c.s0 = (float)a.critical_stretch;
-    c.s0_err = 6.0e-8f * fabsf(c.s0);
-    c.dt_hi = (float)a.dt;
-    c.dt_lo = (float)(a.dt - (double)c.dt_hi);
-    const double half = a.dt / 2;
-    c.half_hi = (float)half;
-    c.half_lo = (float)(half - (double)c.half_hi);
-    c.damping = (float)a.damping;
-    return c;
-}
-
-int sm_count() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            n = 1;
-    }
-    return n;
-}
-
-// Persistent launch: as many CTAs as fit on the device at once (cached per
-// kernel instance and shared-memory size).
-template <int SL, bool CORR, bool TYPES, int MINB>
-int launch_instance(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
-    auto kernel = k_mixed<SL, CORR, TYPES, MINB>;
-    const size_t smem =
-        sizeof(MixedShared) + (SL >= 2 ? 2 * (size_t)kChunk * a.max_neigh * sizeof(int32_t) : 0);
-    static size_t cached_smem = 0;
-    static int cached_grid = 0;
-    if (cached_smem != smem) {
-        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess)
-            return PP_ERROR_CUDA;
-        int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarps * 32, smem) !=
-                cudaSuccess ||
-            per_sm < 1)
-            return PP_ERROR_CUDA;
-        cached_grid = per_sm * sm_count();
-        cached_smem = smem;
-    }
-    const int nchunks = (a.nnodes + kChunk - 1) / kChunk;
-    const int grid = nchunks < cached_grid ? nchunks : cached_grid;
-    kernel<<<grid, kWarps * 32, smem, st>>>(a, mixed_const(a), parity, l);
-    return launch_status();
-}
-
-// variant 0: register budget for 2 resident CTAs per SM, 1: for 3.
-template <int SL, bool CORR, bool TYPES>
-int launch_variant(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
-    if (a.variant == 1) return launch_instance<SL, CORR, TYPES, 3>(a, parity, l, st);
-    return launch_instance<SL, CORR, TYPES, 2>(a, parity, l, st);
-}
-
-template <int SL>
-int launch_sl(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
-    const bool corr = a.stiffness_corrections != nullptr;
-    const bool types = a.bond_types != nullptr;
-    if (!corr && !types) return launch_variant<SL, false, false>(a, parity, l, st);
-    if (corr && !types) return launch_variant<SL, true, false>(a, parity, l, st);
-    if (!corr && types) return launch_variant<SL, false, true>(a, parity, l, st);
-    return launch_variant<SL, true, true>(a, parity, l, st);
-}
 
 // ------------------------------------------------------ pack / export
 __global__ void k_mixed_pack(pp_fused_args a, int parity) {
@@ -634,8 +107,10 @@ __global__ void k_bond_extent(const int32_t* __restrict__ nlist, const double* _
 }
 
 }  // namespace
+}  // namespace mixed
 
 int validate_mixed(const pp_fused_args& a) {
+    using mixed::kMaxTable;
     if (!a.pos_q || !a.uhi[0] || !a.uhi[1] || !a.ulo[0] || !a.ulo[1] || !a.frc || !a.nflags)
         return PP_ERROR_INVALID_VALUE;
     if (!aligned16(a.pos_q) || !aligned16(a.uhi[0]) || !aligned16(a.uhi[1]) ||
@@ -649,22 +124,23 @@ int validate_mixed(const pp_fused_args& a) {
     if (!a.umax || !a.status) return PP_ERROR_INVALID_VALUE;
     if (a.max_neigh > 256) return PP_ERROR_UNSUPPORTED;
     if (a.max_neigh >= 64 && !aligned16(a.nlist)) return PP_ERROR_MISALIGNED;  // bulk copies
+    if (a.node_instance && a.ninstances > kMaxTable) return PP_ERROR_UNSUPPORTED;
     return PP_SUCCESS;
 }
 
 int launch_mixed_step(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
-    switch (a.max_neigh > 32 ? a.max_neigh / 32 : 1) {
-        case 1: return launch_sl<1>(a, parity, l, st);
-        case 2: return launch_sl<2>(a, parity, l, st);
-        case 4: return launch_sl<4>(a, parity, l, st);
-        case 8: return launch_sl<8>(a, parity, l, st);
+    switch (a.variant) {
+        case 0: return mixed::launch_mixed_shape0(a, parity, l, st);
+        case 1: return mixed::launch_mixed_shape1(a, parity, l, st);
+        case 2: return mixed::launch_mixed_shape2(a, parity, l, st);
     }
-    return PP_ERROR_UNSUPPORTED;  // max_neigh > 256
+    return PP_ERROR_INVALID_VALUE;
 }
 
 }  // namespace pp
 
 using namespace pp;
+using namespace pp::mixed;
 
 extern "C" int pp_bond_extent(const int32_t* nlist, const double* r0, int32_t nnodes,
                               int32_t max_neigh, double* extent, void* stream) {

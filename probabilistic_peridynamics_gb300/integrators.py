@@ -186,6 +186,27 @@ class _CUDAIntegrator(Integrator):
         self.damping = 0.0
         self._parity = 0
         self._fargs = None
+        self._instances = None
+
+    def set_instances(self, node_instance, instance_critical_stretch):
+        """Step many independent models at once (see :mod:`.batch`).
+
+        Node ``i`` breaks its bonds at
+        ``instance_critical_stretch[node_instance[i]]`` instead of the
+        scalar critical stretch.  Fused integrators and the PMB damage model
+        only; call before :meth:`build`.
+        """
+        if not self.fused:
+            raise ValueError("instances need a fused integrator")
+        node_instance = np.ascontiguousarray(node_instance, dtype=np.intc)
+        s0 = np.ascontiguousarray(instance_critical_stretch,
+                                  dtype=np.float64).ravel()
+        if not 1 <= s0.size <= 256:
+            raise ValueError("between 1 and 256 instances are supported")
+        if node_instance.size and (node_instance.min() < 0
+                                   or node_instance.max() >= s0.size):
+            raise ValueError("node_instance out of range")
+        self._instances = (node_instance, s0)
 
     # -------------------------------------------------------------- helpers
     def _dev(self, array, dtype):
@@ -248,6 +269,16 @@ class _CUDAIntegrator(Integrator):
             else self._dev(stiffness_corrections, np.float64))
         self.bond_types_d = (None if bond_types is None
                              else self._dev(bond_types, np.int32))
+        if self._instances is not None:
+            if bond_types is not None:
+                raise ValueError("instances support the PMB damage model "
+                                 "only (no bond types)")
+            if self._instances[0].shape != (self.nnodes,):
+                raise ValueError("node_instance must have nnodes entries")
+            self.node_instance_d = self._dev(self._instances[0], np.int32)
+            self.instance_s0_d = self._dev(self._instances[1], np.float64)
+        else:
+            self.node_instance_d = self.instance_s0_d = None
         if self.bond_types_d is not None and (
                 tuple(self.bond_types_d.shape) != (self.nnodes, mn)):
             raise ValueError("bond_types shape must be (nnodes, "
@@ -303,6 +334,8 @@ class _CUDAIntegrator(Integrator):
                         critical_stretch, plus_cs, u, ud, udd, regimes,
                         nregimes, nbond_types):
         n, mn = self.nnodes, self.max_neighbours
+        if self._instances is not None and (nbond_types != 1 or nregimes != 1):
+            raise ValueError("instances support the PMB damage model only")
         if (nbond_types == 1) and (nregimes == 1):
             self.bond_stiffness_d = np.float64(bond_stiffness)
             self.critical_stretch_d = np.float64(critical_stretch)
@@ -418,6 +451,10 @@ class _CUDAIntegrator(Integrator):
         a.densities = _ptr(self.densities_d)
         a.stiffness_corrections = _ptr(self.stiffness_corrections_d)
         a.bond_types = _ptr(self.bond_types_d)
+        if self.node_instance_d is not None:
+            a.node_instance = _ptr(self.node_instance_d)
+            a.instance_s0 = _ptr(self.instance_s0_d)
+            a.ninstances = int(self.instance_s0_d.numel())
         a.nlist = _ptr(self.nlist_d)
         a.regimes = _ptr(self.regimes_d)
         a.u[0] = self.u_d[0].data_ptr()
