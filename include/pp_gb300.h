@@ -280,6 +280,49 @@ int pp_mixed_pack(const pp_fused_args* args, int32_t parity, void* stream);
 int pp_mixed_export(const pp_fused_args* args, int32_t parity, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Adjoint of the Euler step (gradients of a displacement loss).            */
+/* No counterpart in the reference: PeriPy has no gradients.  The forward  */
+/* step is pp_fused_step with PP_FLOAT64, PP_EULER, stiffness corrections   */
+/* = per-bond stiffness k_b, bond_stiffness = 1 and critical_stretch =      */
+/* +inf (the bond set is frozen); this is the reverse of that step.         */
+/* ------------------------------------------------------------------------ */
+
+typedef struct pp_adjoint_args {
+    int32_t nnodes;
+    int32_t max_neigh;             /* power of two, 1..1024               */
+    double dt;
+    const double* r0;              /* (nnodes,3)                           */
+    const double* vols;            /* (nnodes)                             */
+    const int32_t* nlist;          /* (nnodes,max_neigh), -1 = no bond     */
+    const int32_t* partner;        /* from pp_partner_slots                */
+    const int32_t* bc_types;       /* (nnodes,3): nonzero = prescribed DOF */
+    const double* stiffness;       /* (nnodes,max_neigh) per-bond k_b      */
+} pp_adjoint_args;
+
+/* partner[i][s] = the slot of i in row nlist[i][s] (or -1): where the
+ * reverse bond's data lives. */
+int pp_partner_slots(const int32_t* nlist, int32_t nnodes, int32_t max_neigh,
+                     int32_t* partner, void* stream);
+
+/* break_step[g] = t for every slot g with nlist[g] == -1 and
+ * break_step[g] > t: called after forward step t, it records the first step
+ * at which each bond is broken (initialise break_step to INT32_MAX). */
+int pp_mark_breaks(const int32_t* nlist, int32_t* break_step, int64_t nslots,
+                   int32_t t, void* stream);
+
+/* nlist_t[g] = break_step[g] > t ? nlist0[g] : -1: the bond set in force
+ * during step t, frozen for recomputation and the reverse step. */
+int pp_bonds_at_step(const int32_t* nlist0, const int32_t* break_step,
+                     int64_t nslots, int32_t t, int32_t* nlist_t, void* stream);
+
+/* One reverse step: from lam_next = dL/du_{t+1} and the state u = u_t,
+ * writes lam = dL/du_t and adds dL/dk_b of this step to grad_k
+ * ((nnodes,max_neigh)). */
+int pp_adjoint_backward(const pp_adjoint_args* args, const double* u,
+                        const double* lam_next, double* lam, double* grad_k,
+                        void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Fused steps without any device allocation.                               */
 /* ------------------------------------------------------------------------ */
 

@@ -82,6 +82,16 @@ class FusedArgs(ctypes.Structure):
     ]
 
 
+class AdjointArgs(ctypes.Structure):
+    """Mirror of ``pp_adjoint_args``."""
+
+    _fields_ = [
+        ("nnodes", _i32), ("max_neigh", _i32), ("dt", _f64),
+        ("r0", _vp), ("vols", _vp), ("nlist", _vp), ("partner", _vp),
+        ("bc_types", _vp), ("stiffness", _vp),
+    ]
+
+
 #: Every symbol the header declares, with (restype, argtypes).
 SIGNATURES = {
     "pp_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -105,6 +115,11 @@ SIGNATURES = {
     "pp_bond_extent": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
     "pp_mixed_pack": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
     "pp_mixed_export": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
+    "pp_partner_slots": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp]),
+    "pp_mark_breaks": (ctypes.c_int, [_vp, _vp, _i64, _i32, _vp]),
+    "pp_bonds_at_step": (ctypes.c_int, [_vp, _vp, _i64, _i32, _vp, _vp]),
+    "pp_adjoint_backward": (
+        ctypes.c_int, [ctypes.POINTER(AdjointArgs), _vp, _vp, _vp, _vp, _vp]),
     "pp_fused_run_static": (
         ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _i64, _vp, _vp, _vp]),
     "pp_static_status": (ctypes.c_int, [_vp, _vp]),
