@@ -142,6 +142,8 @@ def _rollout_function():
         @staticmethod
         def forward(ctx, stiffness, critical_stretch, problem, steps,
                     checkpoint_every):
+            caller = torch.cuda.current_stream(problem.context.device)
+            problem.context.stream.wait_stream(caller)
             with problem.context.on_stream():
                 k = stiffness.detach().to(torch.float64).contiguous()
                 s0 = float(critical_stretch)
@@ -157,6 +159,9 @@ def _rollout_function():
                     check(lib().pp_mark_breaks(_p(nl), _p(breaks), nl.numel(),
                                                t, problem._stream),
                           "pp_mark_breaks")
+            # the caller's stream may use u only after the rollout
+            caller.wait_stream(problem.context.stream)
+            u.record_stream(caller)
             ctx.problem = problem
             ctx.steps = steps
             ctx.every = checkpoint_every
@@ -170,6 +175,8 @@ def _rollout_function():
         @staticmethod
         def backward(ctx, grad_u):
             problem = ctx.problem
+            caller = torch.cuda.current_stream(problem.context.device)
+            problem.context.stream.wait_stream(caller)
             with problem.context.on_stream():
                 lam = grad_u.detach().to(torch.float64).contiguous()
                 grad_k = torch.zeros_like(ctx.k)
@@ -186,8 +193,14 @@ def _rollout_function():
                         problem.bonds_at_step(ctx.breaks, t, nl_t)
                         lam = problem.backward_step(states[t - t0], lam,
                                                     grad_k, ctx.k, nl_t)
-                grad_s0 = torch.zeros_like(ctx.s0_like, dtype=torch.float64)
-            return (grad_k.to(ctx.param_dtype), grad_s0, None, None, None)
+                # frozen breaks: the loss does not depend on the critical
+                # stretch between breaks
+                grad_s0 = (torch.zeros_like(ctx.s0_like, dtype=torch.float64)
+                           if ctx.needs_input_grad[1] else None)
+                grad_k = grad_k.to(ctx.param_dtype)
+            caller.wait_stream(problem.context.stream)
+            grad_k.record_stream(caller)
+            return (grad_k, grad_s0, None, None, None)
 
     return Rollout
 

@@ -1,9 +1,15 @@
 """Adjoint of the Euler rollout (GPU).
 
-* Central finite differences (relative step 1e-4) on 32 random bonds of the
-  50x50x5 lattice after 500 Euler steps, loss = sum of squared displacements
-  of 100 seeded probe nodes, checkpoint every 50 steps: relative agreement
-  better than 1e-5.
+* Central finite differences (relative step 1e-3) on 32 random bonds of the
+  50x50x5 lattice after 500 Euler steps pulled at 1e-5 per step, loss = sum
+  of squared displacements of 100 seeded probe nodes, checkpoint every 50
+  steps: relative agreement better than 1e-6.  The difference quotient is
+  limited by rounding, not truncation: the stretch (|p| - |xi|)/|xi| loses
+  log10(1/s) digits to cancellation, so its error grows as the strain or the
+  step shrinks (measured on 8 bonds: at a pull of 1e-9 per step the error
+  is 1e-4 at step 1e-3 and 6e-3 at step 1e-5; at 1e-5 per step it is 1e-8
+  at step 1e-3 and 1e-5 at step 1e-6).  Bonds are drawn among those whose
+  gradient is at least 1e-2 of the largest.
 * An FP64 torch-autograd restatement of the same forward (breaking included,
   the break pattern frozen as the adjoint freezes it) on a smaller lattice
   whose bonds break: gradients agree to 1e-9 relative.
@@ -50,7 +56,7 @@ def _stiffness(nlist, seed, torch):
 def test_adjoint_vs_central_differences(torch):
     from probabilistic_peridynamics_gb300.adjoint import rollout
     steps, every = 500, 50
-    prob, coords, _, nlist, *_ = _problem(50, 50, 5, steps, 1e-9)
+    prob, coords, _, nlist, *_ = _problem(50, 50, 5, steps, 1e-5)
     rng = np.random.default_rng(4)
     probes = torch.tensor(rng.choice(coords.shape[0], 100, replace=False),
                           device="cuda")
@@ -64,9 +70,14 @@ def test_adjoint_vs_central_differences(torch):
     L = loss(k)
     L.backward()
     grad = k.grad.detach().cpu().numpy()
-    valid = np.argwhere(nlist != -1)
-    picks = valid[rng.choice(len(valid), 32, replace=False)]
-    eps = 1e-4
+    # Central differences resolve a bond's gradient only above the rounding
+    # noise of the loss: draw the 32 random bonds among those whose
+    # gradient is at least 1e-2 of the largest.
+    significant = np.argwhere((nlist != -1) &
+                              (np.abs(grad) >= 1e-2 * np.abs(grad).max()))
+    assert len(significant) >= 32
+    picks = significant[rng.choice(len(significant), 32, replace=False)]
+    eps = 1e-3
     with torch.no_grad():
         for i, s in picks:
             h = eps * float(k[i, s])
@@ -76,8 +87,7 @@ def test_adjoint_vs_central_differences(torch):
             km[i, s] -= h
             fd = (float(loss(kp)) - float(loss(km))) / (2 * h)
             g = grad[i, s]
-            assert abs(fd - g) <= 1e-5 * max(abs(fd), 1e-30) + 1e-30, \
-                (i, s, fd, g)
+            assert abs(fd - g) <= 1e-6 * abs(fd), (i, s, fd, g)
     # critical stretch: frozen breaks, zero gradient and zero FD (nothing
     # breaks at s0 = 1 in this elastic run)
     assert float(s0.grad) == 0.0
@@ -132,7 +142,8 @@ def test_adjoint_vs_fp64_autograd_with_breaks(torch):
     u = rollout(k, s0, prob, steps, checkpoint_every=7)
     (w * u ** 2).sum().backward()
     scale = float(k_ref.grad.abs().max())
-    assert float((u - u_ref).abs().max()) <= 1e-12 * float(u_ref.abs().max())
+    assert float((u - u_ref).detach().abs().max()) <= \
+        1e-12 * float(u_ref.detach().abs().max())
     assert float((k.grad - k_ref.grad).abs().max()) <= 1e-9 * scale
 
 
