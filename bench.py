@@ -82,7 +82,7 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--accuracy-steps", type=int, default=E2E_STEPS)
-    p.add_argument("--workload", choices=["large", "batched"],
+    p.add_argument("--workload", choices=["large", "batched", "composite"],
                    default="large",
                    help="large: the 200x200x10 Velocity-Verlet plate (the "
                         "headline); batched: 64 uneven UQ instances, "
@@ -214,9 +214,9 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ measurements
-def time_steps(integ, steps, warmup, torch, dist=None):
+def time_steps(integ, steps, warmup, torch, dist=None, rate=PULL_RATE):
     """Device time of exactly ``steps`` fused steps (graph replays)."""
-    dm = torch.as_tensor(PULL_RATE * np.arange(1, warmup + steps + 1),
+    dm = torch.as_tensor(rate * np.arange(1, warmup + steps + 1),
                          dtype=torch.float64, device=integ.context.device)
     fm = torch.zeros_like(dm)
     stream = integ.context.stream
@@ -238,14 +238,15 @@ def time_steps(integ, steps, warmup, torch, dist=None):
     return e0.elapsed_time(e1)
 
 
-def time_kernel_launches(integ, nlaunch, torch, first_mag=0.0):
+def time_kernel_launches(integ, nlaunch, torch, first_mag=0.0,
+                         rate=PULL_RATE):
     """Mean duration of individual fused-step launches (events per launch)."""
     stream = integ.context.stream
     evs = [(torch.cuda.Event(enable_timing=True),
             torch.cuda.Event(enable_timing=True)) for _ in range(nlaunch)]
     for k, (a, b) in enumerate(evs):
         a.record(stream)
-        integ(first_mag + PULL_RATE * k, 0.0)
+        integ(first_mag + rate * k, 0.0)
         b.record(stream)
     stream.synchronize()
     return statistics.mean(a.elapsed_time(b) for a, b in evs)
@@ -520,6 +521,104 @@ def batched_main(args):
     print(json.dumps(line), flush=True)
 
 
+COMPOSITE_RATE = 5e-7
+
+
+def composite_main(args):
+    """The irregular composite: 1M Poisson-disk points in 2.0 x 1.0 x 0.1,
+    horizon 0.012, bond types 0/1/2 (K = 1e9, 3e9, harmonic-mean interface),
+    trilinear damage (0.004, 0.006, 0.01), Velocity-Verlet with density
+    2400, damping 2.5e6, dt 1e-6, x faces pulled 5e-7 per step; mixed step
+    with compensated force sums, its error against the FP64 step after
+    ``--accuracy-steps`` steps with and without compensation."""
+    import torch
+    import probabilistic_peridynamics_gb300 as pp
+    from probabilistic_peridynamics_gb300.pointset import composite
+    t0 = time.perf_counter()
+    w = composite()
+    setup_s = time.perf_counter() - t0
+    n = w["coords"].shape[0]
+    bonds = int(w["family"].sum())
+
+    def make(precision, compensated=False):
+        integ = pp.VelocityVerletCUDA(DAMPING, dt=DT, precision=precision,
+                                      compensated=compensated)
+        integ.build(n, 3, w["max_neigh"], w["coords"], w["volume"],
+                    w["family"], w["bc_types"], w["bc_values"],
+                    np.zeros((n, 3), dtype=np.intc), np.zeros((n, 3)), None,
+                    w["bond_types"], w["densities"])
+        z = np.zeros((n, 3))
+        integ.create_buffers(w["nlist"], w["n_neigh"], w["bond_stiffness"],
+                             w["critical_stretch"], w["plus_cs"], z, z, z, z,
+                             z, np.zeros(n), None, w["nregimes"],
+                             w["nbond_types"])
+        return integ
+
+    integ = make("mixed", compensated=True)
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms = time_steps(integ, args.steps, args.warmup, torch,
+                    rate=COMPOSITE_RATE)
+    clk = clocks.stop()
+    kernel_ms = time_kernel_launches(integ, 100, torch, rate=COMPOSITE_RATE)
+    tuning, variant = integ.tuning, int(integ._fargs.variant)
+    del integ
+    torch.cuda.empty_cache()
+    acc = None
+    if args.accuracy_steps:
+        steps = args.accuracy_steps
+        mags = COMPOSITE_RATE * np.arange(1, steps + 1)
+        res = {}
+        for name, prec, comp in (("fp64", "float64", False),
+                                 ("mixed", "mixed", False),
+                                 ("mixed_compensated", "mixed", True)):
+            it = make(prec, comp)
+            it._run(mags, np.zeros(steps), 0, steps)
+            z = [np.zeros((n, 3)) for _ in range(5)]
+            res[name] = it.write(*z, np.zeros(n), w["nlist"].copy(),
+                                 w["n_neigh"].copy())
+            del it
+            torch.cuda.empty_cache()
+        u64, nl64 = res["fp64"][0], res["fp64"][6]
+        acc = {"steps": steps,
+               "bonds_broken_fp64": int((w["nlist"] != -1).sum() -
+                                        (nl64 != -1).sum()),
+               "max_abs_u": float(np.abs(u64).max())}
+        for name in ("mixed", "mixed_compensated"):
+            u = res[name][0]
+            acc[name] = {
+                "disp_rel_err_vs_fp64": float(np.abs(u - u64).max() /
+                                              np.abs(u64).max()),
+                "mask_flips_vs_fp64": int((res[name][6] != nl64).sum())}
+    peaks = load_peaks()
+    peak = float(peaks["hbm_gbs"]) if peaks else 6800.0
+    # int32 nlist + bond_types + regimes per bond; VV node bytes
+    alg = bonds * (4 + 4 + 4) + n * B_NODE_VV
+    achieved = alg / (kernel_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": bonds * args.steps / (ms * 1e-3),
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "irregular composite: 1M Poisson-disk points "
+                               "in 2.0x1.0x0.1, 3 bond types, trilinear "
+                               "damage, Velocity-Verlet",
+                   "nodes": n, "bonds": bonds, "max_neigh": w["max_neigh"],
+                   "setup_s": setup_s, "pull_rate": COMPOSITE_RATE,
+                   "precision": "mixed, compensated force sums",
+                   "tile_shape_autotune_ms": tuning, "variant": variant},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "algorithmic_bytes_per_launch": alg,
+                     "kernel_ms": kernel_ms},
+        "gpu_launches": args.steps + (args.steps // 16 + 1
+                                      if args.steps >= 32 else 0),
+        "clocks": clk, "accuracy": acc,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.profile:
@@ -530,6 +629,9 @@ def main():
         return
     if args.workload == "batched":
         batched_main(args)
+        return
+    if args.workload == "composite":
+        composite_main(args)
         return
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -56,7 +56,10 @@ extern "C" {
                                           step's results are invalid     */
 
 /* Flags of the fused step. */
-#define PP_FLAG_COMPENSATED         1  /* compensated (TwoSum) FP32 force sum */
+#define PP_FLAG_COMPENSATED         1  /* PP_MIXED only: compensated FP32 force
+                                          sums (FMA product error + TwoSum,
+                                          carried through the warp reduction);
+                                          PP_ERROR_UNSUPPORTED with PP_FLOAT64 */
 
 /* ------------------------------------------------------------------------ */
 /* Utility.                                                                 */
@@ -181,7 +184,7 @@ typedef struct pp_fused_args {
     int32_t precision;             /* PP_FLOAT64 / PP_MIXED                */
     int32_t nregimes;
     int32_t nbond_types;
-    int32_t flags;
+    int32_t flags;                 /* PP_FLAG_* bits; others must be 0     */
     int32_t nodes_per_block;       /* PP_FLOAT64: warps per block (0 = 8)  */
     int32_t variant;               /* PP_MIXED tile shape, 0..PP_MIXED_VARIANTS-1:
                                       0: 8 warps x 64 nodes per CTA, register

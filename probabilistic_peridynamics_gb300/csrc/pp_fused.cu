@@ -96,6 +96,9 @@ int validate_fused(const pp_fused_args& a) {
     if (a.integrator < PP_EULER || a.integrator > PP_VELOCITY_VERLET) return PP_ERROR_INVALID_VALUE;
     if (a.nodes_per_block < 0 || a.nodes_per_block > 32) return PP_ERROR_INVALID_VALUE;
     if (a.reserved != 0 || a.reserved2 != 0) return PP_ERROR_INVALID_VALUE;
+    if (a.flags & ~PP_FLAG_COMPENSATED) return PP_ERROR_INVALID_VALUE;
+    // compensation applies to the FP32 force sums of PP_MIXED only
+    if ((a.flags & PP_FLAG_COMPENSATED) && a.precision != PP_MIXED) return PP_ERROR_UNSUPPORTED;
     if (a.node_instance &&
         (a.bond_types || !a.instance_s0 || a.ninstances < 1 || a.ninstances > 256))
         return PP_ERROR_INVALID_VALUE;

@@ -181,6 +181,53 @@ __device__ __forceinline__ float reduce4(float x, float y, float z, float w, int
     return v;
 }
 
+// Compensated accumulation s + c += a * b: the rounding error of the
+// product (FMA) and of the sum (TwoSum, Knuth) go to the carry c.
+template <bool COMP>
+__device__ __forceinline__ void acc_mul(float& s, float& c, float a, float b) {
+    if constexpr (COMP) {
+        const float t = __fmul_rn(a, b);
+        const float pe = fmaf(a, b, -t);
+        const float ns = __fadd_rn(s, t);
+        const float bp = __fsub_rn(ns, s);
+        const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(ns, bp)), __fsub_rn(t, bp));
+        c = __fadd_rn(c, __fadd_rn(e, pe));
+        s = ns;
+    } else {
+        s = fmaf(a, b, s);
+    }
+}
+
+// (v, c) += (w, d) with the rounding error of v + w added to the carry.
+__device__ __forceinline__ void two_sum_into(float& v, float& c, float w, float d) {
+    const float ns = __fadd_rn(v, w);
+    const float bp = __fsub_rn(ns, v);
+    const float e = __fadd_rn(__fsub_rn(v, __fsub_rn(ns, bp)), __fsub_rn(w, bp));
+    c = __fadd_rn(c, __fadd_rn(d, e));
+    v = ns;
+}
+
+// reduce4 on compensated pairs (x + cx, ...): the same lane layout, the
+// result rounded once at the end.
+__device__ __forceinline__ float reduce4c(float x, float cx, float y, float cy, float z,
+                                          float cz, float w, int lane) {
+    const bool up16 = lane & 16;
+    float a = up16 ? z : x, ac = up16 ? cz : cx;
+    float b = up16 ? w : y, bc = up16 ? 0.f : cy;
+    const float as = up16 ? x : z, asc = up16 ? cx : cz;
+    const float bs = up16 ? y : w, bsc = up16 ? cy : 0.f;
+    two_sum_into(a, ac, __shfl_xor_sync(kFull, as, 16), __shfl_xor_sync(kFull, asc, 16));
+    two_sum_into(b, bc, __shfl_xor_sync(kFull, bs, 16), __shfl_xor_sync(kFull, bsc, 16));
+    const bool up8 = lane & 8;
+    float v = up8 ? b : a, vc = up8 ? bc : ac;
+    two_sum_into(v, vc, __shfl_xor_sync(kFull, up8 ? a : b, 8),
+                 __shfl_xor_sync(kFull, up8 ? ac : bc, 8));
+#pragma unroll
+    for (int off = 4; off >= 1; off >>= 1)
+        two_sum_into(v, vc, __shfl_xor_sync(kFull, v, off), __shfl_xor_sync(kFull, vc, off));
+    return __fadd_rn(v, vc);
+}
+
 constexpr uint32_t kWaitPolls = 1u << 22;  // bound on mbarrier polls
 
 template <int CH>
@@ -192,8 +239,9 @@ struct alignas(16) MixedShared {
 };
 
 // Bond phase of one node (one warp): returns nothing, parks the reduced
-// (force x, y, z, intact count) of local node li in sh.frc[li].
-template <int SL, bool CORR, bool TYPES, class Shared>
+// (force x, y, z, intact count) of local node li in sh.frc[li].  COMP:
+// compensated force sums (acc_mul, reduce4c).
+template <int SL, bool CORR, bool TYPES, bool COMP, class Shared>
 __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const MixedConst& c,
                                                 const QuickBand& qb, Shared& sh,
                                                 const int32_t* nl_row, int parity, int i,
@@ -242,6 +290,7 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
         }
     }
     float sx = 0.f, sy = 0.f, sz = 0.f;
+    float cx = 0.f, cy = 0.f, cz = 0.f;  // carries (COMP)
     float cnt = 0.f;
     unsigned amb = 0u;
 #pragma unroll
@@ -287,9 +336,9 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
         }
         float fv = w * b.ry;
         if constexpr (CORR) fv *= sc[k];
-        sx = fmaf(fv, b.px, sx);
-        sy = fmaf(fv, b.py, sy);
-        sz = fmaf(fv, b.pz, sz);
+        acc_mul<COMP>(sx, cx, fv, b.px);
+        acc_mul<COMP>(sy, cy, fv, b.py);
+        acc_mul<COMP>(sz, cz, fv, b.pz);
         cnt += 1.0f;
     }
     // Slow path: slots whose FP32 stretch is too close to a critical stretch
@@ -320,13 +369,17 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
             }
             float fv = w * b.ry;
             if constexpr (CORR) fv *= sc[k];
-            sx = fmaf(fv, b.px, sx);
-            sy = fmaf(fv, b.py, sy);
-            sz = fmaf(fv, b.pz, sz);
+            acc_mul<COMP>(sx, cx, fv, b.px);
+            acc_mul<COMP>(sy, cy, fv, b.py);
+            acc_mul<COMP>(sz, cz, fv, b.pz);
             cnt += 1.0f;
         }
     }
-    const float v = reduce4(sx, sy, sz, cnt, lane);
+    float v;
+    if constexpr (COMP)
+        v = reduce4c(sx, cx, sy, cy, sz, cz, cnt, lane);
+    else
+        v = reduce4(sx, sy, sz, cnt, lane);
     if ((lane & 7) == 0) reinterpret_cast<float*>(&sh.frc[li])[lane >> 3] = v;
 }
 
@@ -401,7 +454,7 @@ __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedCo
 // One CTA of W warps loops over chunks of 8*W nodes.  For SL >= 2 the chunk's
 // neighbour-list rows (contiguous) stream into shared memory by bulk copy,
 // double-buffered one chunk ahead; for SL == 1 they are read in place.
-template <int SL, bool CORR, bool TYPES, int W, int MINB>
+template <int SL, bool CORR, bool TYPES, bool COMP, int W, int MINB>
 __global__ void __launch_bounds__(W * 32, MINB)
     k_mixed(pp_fused_args a, MixedConst c, int parity, Launch l) {
     constexpr int kChunk = kNodesPerWarp * W;
@@ -475,7 +528,7 @@ __global__ void __launch_bounds__(W * 32, MINB)
             if (i >= a.nnodes) break;  // warp-uniform
             const int32_t* nl_row = kBulk ? s_nl + (size_t)buf * kChunk * L + (size_t)li * L
                                           : a.nlist + (int64_t)i * L;
-            bond_phase_node<SL, CORR, TYPES>(a, c, qb, sh, nl_row, parity, i, li, lane);
+            bond_phase_node<SL, CORR, TYPES, COMP>(a, c, qb, sh, nl_row, parity, i, li, lane);
         }
         __syncthreads();
         node_phase(a, c, sh, m, parity, node0);
@@ -513,10 +566,10 @@ inline int sm_count() {
 
 // Persistent launch: as many CTAs as fit on the device at once (cached per
 // kernel instance and shared-memory size).
-template <int SL, bool CORR, bool TYPES, int W, int MINB>
+template <int SL, bool CORR, bool TYPES, bool COMP, int W, int MINB>
 int launch_instance(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
     constexpr int kChunk = kNodesPerWarp * W;
-    auto kernel = k_mixed<SL, CORR, TYPES, W, MINB>;
+    auto kernel = k_mixed<SL, CORR, TYPES, COMP, W, MINB>;
     const size_t smem = sizeof(MixedShared<kChunk>) +
                         (SL >= 2 ? 2 * (size_t)kChunk * a.max_neigh * sizeof(int32_t) : 0);
     static size_t cached_smem = 0;
@@ -540,17 +593,17 @@ int launch_instance(const pp_fused_args& a, int parity, const Launch& l, cudaStr
 }
 
 // All kernel instances of one tile shape (W warps, register budget MINB).
-template <int W, int MINB>
-int launch_shape(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
+template <int W, int MINB, bool COMP>
+int launch_shape_comp(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
     const bool corr = a.stiffness_corrections != nullptr;
     const bool types = a.bond_types != nullptr;
     const int sl = a.max_neigh > 32 ? a.max_neigh / 32 : 1;
-#define PP_LAUNCH_SL(S)                                                               \
-    if (sl == S) {                                                                    \
-        if (!corr && !types) return launch_instance<S, false, false, W, MINB>(a, parity, l, st); \
-        if (corr && !types) return launch_instance<S, true, false, W, MINB>(a, parity, l, st);  \
-        if (!corr && types) return launch_instance<S, false, true, W, MINB>(a, parity, l, st);  \
-        return launch_instance<S, true, true, W, MINB>(a, parity, l, st);                       \
+#define PP_LAUNCH_SL(S)                                                                      \
+    if (sl == S) {                                                                           \
+        if (!corr && !types) return launch_instance<S, false, false, COMP, W, MINB>(a, parity, l, st); \
+        if (corr && !types) return launch_instance<S, true, false, COMP, W, MINB>(a, parity, l, st);  \
+        if (!corr && types) return launch_instance<S, false, true, COMP, W, MINB>(a, parity, l, st);  \
+        return launch_instance<S, true, true, COMP, W, MINB>(a, parity, l, st);                       \
     }
     PP_LAUNCH_SL(1)
     PP_LAUNCH_SL(2)
@@ -558,6 +611,13 @@ int launch_shape(const pp_fused_args& a, int parity, const Launch& l, cudaStream
     PP_LAUNCH_SL(8)
 #undef PP_LAUNCH_SL
     return PP_ERROR_UNSUPPORTED;  // max_neigh > 256
+}
+
+// All kernel instances of one tile shape (W warps, register budget MINB).
+template <int W, int MINB>
+int launch_shape(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
+    if (a.flags & PP_FLAG_COMPENSATED) return launch_shape_comp<W, MINB, true>(a, parity, l, st);
+    return launch_shape_comp<W, MINB, false>(a, parity, l, st);
 }
 
 // Launchers of the tile shapes, one translation unit each (pp_mixed_v*.cu).

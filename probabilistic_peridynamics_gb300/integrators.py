@@ -176,6 +176,9 @@ class _CUDAIntegrator(Integrator):
         if precision == "mixed" and not fused:
             raise ValueError("precision='mixed' is implemented by the fused "
                              "kernel only; use fused=True")
+        if compensated and precision != "mixed":
+            raise ValueError("compensated=True applies to the FP32 force sums "
+                             "of precision='mixed'")
         self.fused = bool(fused)
         self.precision = precision
         self.compensated = bool(compensated)

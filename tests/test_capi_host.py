@@ -92,6 +92,15 @@ def test_validation_without_gpu(L):
     fa.precision = 9
     assert L.pp_fused_step(ctypes.byref(fa), 0, 0.0, 0.0, None) == \
         _lib.PP_ERROR_INVALID_VALUE
+    # flags: unknown bits, and compensation outside PP_MIXED
+    fa.precision = _lib.PP_FLOAT64
+    fa.flags = 2
+    assert L.pp_fused_step(ctypes.byref(fa), 0, 0.0, 0.0, None) == \
+        _lib.PP_ERROR_INVALID_VALUE
+    fa.flags = _lib.PP_FLAG_COMPENSATED
+    assert L.pp_fused_step(ctypes.byref(fa), 0, 0.0, 0.0, None) == \
+        _lib.PP_ERROR_UNSUPPORTED
+    fa.flags = 0
     # misaligned mixed-precision pointers are rejected before any launch
     buf = (ctypes.c_char * 64)()
     base = ctypes.addressof(buf)
