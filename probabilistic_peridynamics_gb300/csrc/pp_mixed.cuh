@@ -236,16 +236,38 @@ struct alignas(16) MixedShared {
     float4 frc[CH];
     float thr[kMaxTable], k[kMaxTable], c[kMaxTable];  // regime tables or
                                                         // instance thresholds
+    float tlo[kMaxTable], thi[kMaxTable];              // Thresholds of thr[]
 };
+
+// Stretch thresholds that decide a bond against critical stretch s0 without
+// its own band: s < lo is intact and s > hi broken for every bond of the
+// step, from |s - s0| > quick.a + quick.c |s| + s0err solved for s (both
+// signs of s), widened by 5e-7 relative to cover their own rounding.
+struct Thresholds {
+    float lo, hi;
+};
+
+__device__ __forceinline__ Thresholds thresholds(float s0f, float s0err, const QuickBand& q) {
+    const float x = s0f - q.a - s0err;  // s < s0 side
+    const float y = s0f + q.a + s0err;  // s > s0 side
+    float lo = x >= 0.0f ? x / (1.0f + q.c) : x / (1.0f - q.c);
+    float hi = y > 0.0f ? y / (1.0f - q.c) : y / (1.0f + q.c);
+    lo -= fmaf(fabsf(lo), 5.0e-7f, 1.0e-30f);
+    hi += fmaf(fabsf(hi), 5.0e-7f, 1.0e-30f);
+    return {lo, hi};
+}
 
 // Bond phase of one node (one warp): returns nothing, parks the reduced
 // (force x, y, z, intact count) of local node li in sh.frc[li].  COMP:
 // compensated force sums (acc_mul, reduce4c).
+//
+// A broken or padding slot (-1) gathers node 0 instead of branching around
+// the loads; its arithmetic is discarded (weight 0, not counted).
 template <int SL, bool CORR, bool TYPES, bool COMP, class Shared>
 __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const MixedConst& c,
-                                                const QuickBand& qb, Shared& sh,
-                                                const int32_t* nl_row, int parity, int i,
-                                                int li, int lane) {
+                                                const QuickBand& qb, const Thresholds& th0,
+                                                Shared& sh, const int32_t* nl_row, int parity,
+                                                int i, int li, int lane) {
     const int L = a.max_neigh;
     const int nr = a.nregimes;
     const int64_t row = (int64_t)i * L;
@@ -255,11 +277,14 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
     // critical stretch of this node (per instance when batched)
     float s0f = c.s0, s0err = c.s0_err;
     double s0d = a.critical_stretch;
+    Thresholds th = th0;
     if (!TYPES && a.node_instance) {
         const int inst = a.node_instance[i];
         s0f = sh.thr[inst];
         s0err = 6.0e-8f * fabsf(s0f);
         s0d = a.instance_s0[inst];
+        th.lo = sh.tlo[inst];
+        th.hi = sh.thi[inst];
     }
     int jr[SL];
 #pragma unroll
@@ -273,17 +298,11 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
     int bt[SL], rg[SL];
 #pragma unroll
     for (int k = 0; k < SL; ++k) {
-        // An empty slot gets a harmless stand-in (one fixed-point step away,
-        // same displacement) so that all arithmetic stays finite.
-        if (jr[k] != -1) {
-            qj[k] = ldg_i4(a.pos_q, jr[k]);
-            uj[k] = ldg_f4(uhi, jr[k]);
-        } else {
-            qj[k] = make_int4(qi.x + 1, qi.y, qi.z, 0);
-            uj[k] = ui;
-        }
+        const int jj = max(jr[k], 0);
+        qj[k] = ldg_i4(a.pos_q, jj);
+        uj[k] = ldg_f4(uhi, jj);
         const int64_t gid = row + lane + 32 * k;
-        if constexpr (CORR) sc[k] = jr[k] != -1 ? __ldcs(a.sc32 + gid) : 0.f;
+        if constexpr (CORR) sc[k] = __ldcs(a.sc32 + gid);
         if constexpr (TYPES) {
             bt[k] = jr[k] != -1 ? __ldcs(a.bond_types + gid) * nr : 0;
             rg[k] = jr[k] != -1 ? a.regimes[gid] : 0;
@@ -295,30 +314,33 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
     unsigned amb = 0u;
 #pragma unroll
     for (int k = 0; k < SL; ++k) {
-        if (jr[k] == -1) continue;
-        const int64_t gid = row + lane + 32 * k;
+        const bool valid = jr[k] != -1;
         const Bond32 b = bond32(qi, ui, qj[k], uj[k], c);
-        const float quick = fmaf(qb.c, fabsf(b.s), qb.a);
         float w = __int_as_float(qj[k].w);  // k*vol (PMB) or vol (types)
         bool intact;
         if constexpr (!TYPES) {
-            const float d = b.s - s0f;
-            if (!(fabsf(d) > quick + s0err)) {
-                if (!(fabsf(d) > band32(ui, uj[k], b, c) + s0err)) {
-                    amb |= 1u << k;
-                    continue;
-                }
+            intact = b.s < th.lo;
+            bool broken = b.s > th.hi;
+            if (valid && !intact && !broken) {  // near s0: the bond's own band
+                const float d = b.s - s0f;
+                if (!(fabsf(d) > band32(ui, uj[k], b, c) + s0err))
+                    amb |= 1u << k;  // decided on the binary64 stretch below
+                else
+                    intact = d < 0.0f, broken = !intact;
             }
-            intact = d < 0.0f;
+            if (valid && broken) a.nlist[row + lane + 32 * k] = -1;
+            intact = intact && valid;
             w *= b.s;
         } else {
+            if (!valid) continue;
+            const int64_t gid = row + lane + 32 * k;
             bool ambiguous = false;
             const int reg = next_regime(rg[k], bt[k], nr, [&](int idx) {
+                if (b.s < sh.tlo[idx]) return true;
+                if (b.s > sh.thi[idx]) return false;
                 const float thr = sh.thr[idx];
                 const float d = b.s - thr;
-                const float err = 6.0e-8f * fabsf(thr);
-                if (!(fabsf(d) > quick + err) &&
-                    !(fabsf(d) > band32(ui, uj[k], b, c) + err))
+                if (!(fabsf(d) > band32(ui, uj[k], b, c) + 6.0e-8f * fabsf(thr)))
                     ambiguous = true;
                 return d < 0.0f;
             });
@@ -328,18 +350,19 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
             }
             if (reg != rg[k]) a.regimes[gid] = reg;
             intact = reg < nr;
-            if (intact) w *= fmaf(b.s, sh.k[bt[k] + reg], sh.c[bt[k] + reg]);
+            if (!intact) {
+                a.nlist[gid] = -1;
+                continue;
+            }
+            w *= fmaf(b.s, sh.k[bt[k] + reg], sh.c[bt[k] + reg]);
         }
-        if (!intact) {
-            a.nlist[gid] = -1;
-            continue;
-        }
-        float fv = w * b.ry;
+        float fv = intact ? w * b.ry : 0.0f;
         if constexpr (CORR) fv *= sc[k];
-        acc_mul<COMP>(sx, cx, fv, b.px);
-        acc_mul<COMP>(sy, cy, fv, b.py);
-        acc_mul<COMP>(sz, cz, fv, b.pz);
-        cnt += 1.0f;
+        const float px = intact ? b.px : 0.0f;  // finite for discarded slots
+        acc_mul<COMP>(sx, cx, fv, px);
+        acc_mul<COMP>(sy, cy, fv, intact ? b.py : 0.0f);
+        acc_mul<COMP>(sz, cz, fv, intact ? b.pz : 0.0f);
+        cnt += intact ? 1.0f : 0.0f;
     }
     // Slow path: slots whose FP32 stretch is too close to a critical stretch
     // are decided on the binary64 stretch.
@@ -467,17 +490,29 @@ __global__ void __launch_bounds__(W * 32, MINB)
     const int nchunks = (a.nnodes + kChunk - 1) / kChunk;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    // error bounds of this step: running max |u| and the shortest bond
+    const float U = __ldcg(a.umax);
+    const QuickBand qb = quick_band(U, c);
     if constexpr (TYPES) {
         const int nt = a.nbond_types * a.nregimes;
         for (int t = threadIdx.x; t < nt; t += blockDim.x) {
-            sh.thr[t] = (float)a.critical_stretch_table[t];
+            const float thr = (float)a.critical_stretch_table[t];
+            const Thresholds th = thresholds(thr, 6.0e-8f * fabsf(thr), qb);
+            sh.thr[t] = thr;
+            sh.tlo[t] = th.lo;
+            sh.thi[t] = th.hi;
             sh.k[t] = (float)a.bond_stiffness_table[t];
             sh.c[t] = (float)a.plus_cs[t];
         }
     } else {
         if (a.node_instance)
-            for (int t = threadIdx.x; t < a.ninstances; t += blockDim.x)
-                sh.thr[t] = (float)a.instance_s0[t];
+            for (int t = threadIdx.x; t < a.ninstances; t += blockDim.x) {
+                const float thr = (float)a.instance_s0[t];
+                const Thresholds th = thresholds(thr, 6.0e-8f * fabsf(thr), qb);
+                sh.thr[t] = thr;
+                sh.tlo[t] = th.lo;
+                sh.thi[t] = th.hi;
+            }
     }
     uint64_t policy = 0;
     auto issue = [&](int chunk, int buf) {
@@ -501,8 +536,7 @@ __global__ void __launch_bounds__(W * 32, MINB)
         __syncthreads();
     }
     const StepMags m = step_mags(l);
-    const float U = __ldcg(a.umax);
-    const QuickBand qb = quick_band(U, c);
+    const Thresholds th0 = thresholds(c.s0, c.s0_err, qb);
     int it = 0;
     for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x, ++it) {
         const int buf = it & 1;
@@ -528,7 +562,8 @@ __global__ void __launch_bounds__(W * 32, MINB)
             if (i >= a.nnodes) break;  // warp-uniform
             const int32_t* nl_row = kBulk ? s_nl + (size_t)buf * kChunk * L + (size_t)li * L
                                           : a.nlist + (int64_t)i * L;
-            bond_phase_node<SL, CORR, TYPES, COMP>(a, c, qb, sh, nl_row, parity, i, li, lane);
+            bond_phase_node<SL, CORR, TYPES, COMP>(a, c, qb, th0, sh, nl_row, parity, i, li,
+                                                   lane);
         }
         __syncthreads();
         node_phase(a, c, sh, m, parity, node0);
