@@ -150,19 +150,21 @@ int pp_update_displacement_velocity_verlet(
 /* arithmetic is bit-identical to the plain kernels.                        */
 /*                                                                          */
 /* PP_MIXED uses the compact layouts produced by pp_mixed_pack():           */
-/*   pos_q   (nnodes) int4 {qx,qy,qz, w}: fixed-point positions,            */
-/*           r0 = origin + q * pos_scale, pos_scale a power of two with     */
-/*           pos_scale >= 2^-21 * pp_bond_extent() so that every bond's     */
-/*           |q[j] - q[i]| < 2^22 converts to float exactly without an      */
-/*           int-to-float instruction; w = float bits of k*vol (PMB) or of  */
-/*           vol (bond types)                                               */
-/*   uhi[2]  (nnodes) float4 {ux,uy,uz, max|u|}: FP32 displacement (high   */
-/*           part of the double-float pair), gathered by neighbours         */
+/*   rec[2]  (nnodes) 32-byte node records, 32-byte aligned, gathered by    */
+/*           the neighbours of a node with one 256-bit load:               */
+/*           {qx,qy,qz (int32), w, ux,uy,uz, m (float)}.  q: fixed-point    */
+/*           positions, r0 = origin + q * pos_scale, pos_scale a power of   */
+/*           two with pos_scale >= 2^-21 * pp_bond_extent() so that every   */
+/*           bond's |q[j] - q[i]| < 2^22 converts to float exactly without  */
+/*           an int-to-float instruction; w = k*vol (PMB) or vol (bond      */
+/*           types); u = FP32 displacement (high part of the double-float   */
+/*           pair); m = max|u| of the node.  The step reads rec[parity] and */
+/*           writes the whole of rec[parity ^ 1].                           */
 /*   ulo[2]  (nnodes) float4: low parts of the double-float displacement    */
 /*   vel     (nnodes) float4 x2 {hi; lo}: double-float velocity (EC, VV)    */
 /*   acc     (nnodes) float4: FP32 acceleration (EC, VV)                    */
 /*   frc     (nnodes) float4 x2 {force; body_force} FP32                    */
-/*   rho32   (nnodes) float4 FP32 densities (EC, VV)                        */
+/*   rho32   (nnodes) float4 FP32 reciprocal densities 1/rho (EC, VV)       */
 /*   nflags  (nnodes) int: bit d set when bc_types[3i+d] != 0, bit 3+d when  */
 /*           fc_types[3i+d] != 0                                            */
 /*   sc32    (nnodes,max_neigh) float stiffness corrections or NULL         */
@@ -187,10 +189,11 @@ typedef struct pp_fused_args {
     int32_t flags;                 /* PP_FLAG_* bits; others must be 0     */
     int32_t nodes_per_block;       /* PP_FLOAT64: warps per block (0 = 8)  */
     int32_t variant;               /* PP_MIXED tile shape, 0..PP_MIXED_VARIANTS-1:
-                                      0: 8 warps x 64 nodes per CTA, register
-                                      budget for 2 resident CTAs per SM;
-                                      1: 8 warps x 64 nodes, 3 CTAs/SM;
-                                      2: 4 warps x 32 nodes, 6 CTAs/SM   */
+                                      0: 8 warps x 128 nodes per CTA,
+                                      register budget for 3 resident CTAs
+                                      per SM; 1: 8 warps x 128 nodes, 4
+                                      CTAs/SM; 2: 4 warps x 64 nodes, 6
+                                      CTAs/SM                             */
     int32_t reserved;              /* must be 0                            */
     double dt;
     double damping;
@@ -227,14 +230,13 @@ typedef struct pp_fused_args {
     double* body_force;
     int32_t* n_neigh;
     double* damage;
-    /* PP_MIXED node state (16-byte aligned) */
-    int32_t* pos_q;
-    float* uhi[2];
+    /* PP_MIXED node state (16-byte aligned, rec 32-byte aligned) */
+    float* rec[2];                 /* (nnodes) 32-byte node records        */
     float* ulo[2];
     float* vel;                    /* 2*nnodes float4                      */
     float* acc;
     float* frc;                    /* 2*nnodes float4                      */
-    float* rho32;                  /* (nnodes) float4 densities (EC / VV)  */
+    float* rho32;                  /* (nnodes) float4 1/density (EC / VV)  */
     float* sc32;
     int32_t* nflags;               /* (nnodes) boundary-condition flags    */
     float* umax;                   /* device word: running max of |u| (scratch) */
@@ -269,9 +271,10 @@ int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t nsteps,
 int pp_bond_extent(const int32_t* nlist, const double* r0, int32_t nnodes,
                    int32_t max_neigh, double* extent, void* stream);
 
-/* Builds the PP_MIXED layouts from the reference layouts: pos_q from r0 and
- * vols (with args->pos_scale/pos_origin, which the caller chooses), the
- * double-float displacement slot `parity` and velocity from u[parity] and
+/* Builds the PP_MIXED layouts from the reference layouts: rec[parity] from
+ * r0, vols (with args->pos_scale/pos_origin, which the caller chooses) and
+ * u[parity], the double-float displacement slot `parity` and velocity from
+ * u[parity] and
  * ud, acc from udd, sc32 from stiffness_corrections, nflags from bc_types
  * and fc_types.  Called by
  * create_buffers (peripy/integrators.py:190-254). */

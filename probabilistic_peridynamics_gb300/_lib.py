@@ -75,7 +75,7 @@ class FusedArgs(ctypes.Structure):
         ("nlist", _vp), ("regimes", _vp),
         ("u", _vp * 2), ("ud", _vp), ("udd", _vp), ("force", _vp),
         ("body_force", _vp), ("n_neigh", _vp), ("damage", _vp),
-        ("pos_q", _vp), ("uhi", _vp * 2), ("ulo", _vp * 2), ("vel", _vp),
+        ("rec", _vp * 2), ("ulo", _vp * 2), ("vel", _vp),
         ("acc", _vp), ("frc", _vp), ("rho32", _vp), ("sc32", _vp),
         ("nflags", _vp), ("umax", _vp), ("status", _vp),
         ("pos_scale", _f64), ("min_bond", _f64), ("pos_origin", _f64 * 3),

@@ -68,7 +68,7 @@ def tune_mixed(integ, warmup=3, reps=10):
             setattr(scratch, name, clone(getattr(scratch, name),
                                          tensors[name]))
         for k in range(2):
-            scratch.uhi[k] = clone(scratch.uhi[k], integ.uhi_d[k])
+            scratch.rec[k] = clone(scratch.rec[k], integ.rec_d[k])
             scratch.ulo[k] = clone(scratch.ulo[k], integ.ulo_d[k])
         results = {}
         stream = integ.context.stream

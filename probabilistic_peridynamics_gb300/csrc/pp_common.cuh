@@ -140,6 +140,7 @@ __device__ __forceinline__ int4 ldg_i4(const int32_t* p, int64_t i) {
 inline bool is_pow2_le_1024(int32_t x) { return x >= 1 && x <= 1024 && (x & (x - 1)) == 0; }
 
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+inline bool aligned32(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 31u) == 0; }
 
 inline int launch_status() {
     cudaError_t e = cudaGetLastError();

@@ -19,20 +19,21 @@ __global__ void k_mixed_pack(pp_fused_args a, int parity) {
     q.z = (int)llrint((a.r0[o + 2] - a.pos_origin[2]) * inv);
     const double w = a.bond_types ? a.vols[i] : a.bond_stiffness * a.vols[i];
     q.w = __float_as_int((float)w);
-    reinterpret_cast<int4*>(a.pos_q)[i] = q;
+    float* rec = a.rec[parity] + 8 * (int64_t)i;
+    reinterpret_cast<int4*>(rec)[0] = q;
     const double* u = a.u[parity];
     float umax = 0.f;
     int fl = 0;
     for (int d = 0; d < 3; ++d) {
         const df x = df_from_double(u[o + d]);
-        a.uhi[parity][4 * (int64_t)i + d] = x.hi;
+        rec[4 + d] = x.hi;
         a.ulo[parity][4 * (int64_t)i + d] = x.lo;
         umax = fmaxf(umax, fabsf(x.hi));
         fl |= (a.bc_types[o + d] != 0) << d;
         fl |= (a.fc_types[o + d] != 0) << (3 + d);
     }
     a.nflags[i] = fl;
-    a.uhi[parity][4 * (int64_t)i + 3] = umax * (1.0f + 1.2e-7f);
+    rec[7] = umax * (1.0f + 1.2e-7f);
     if (a.umax) atomicMax(reinterpret_cast<int*>(a.umax), __float_as_int(umax * (1.0f + 1.2e-7f)));
     a.ulo[parity][4 * (int64_t)i + 3] = 0.f;
     if (a.vel) {
@@ -41,7 +42,7 @@ __global__ void k_mixed_pack(pp_fused_args a, int parity) {
             a.vel[8 * (int64_t)i + d] = v.hi;
             a.vel[8 * (int64_t)i + 4 + d] = v.lo;
             a.acc[4 * (int64_t)i + d] = a.udd ? (float)a.udd[o + d] : 0.f;
-            a.rho32[4 * (int64_t)i + d] = a.densities ? (float)a.densities[o + d] : 1.f;
+            a.rho32[4 * (int64_t)i + d] = a.densities ? (float)(1.0 / a.densities[o + d]) : 1.f;
         }
         a.vel[8 * (int64_t)i + 3] = 0.f;
         a.vel[8 * (int64_t)i + 7] = 0.f;
@@ -61,7 +62,7 @@ __global__ void k_mixed_export(pp_fused_args a, int parity) {
     const int64_t o = 3 * (int64_t)i;
     for (int d = 0; d < 3; ++d) {
         a.u[parity][o + d] =
-            df_to_double(df{a.uhi[parity][4 * (int64_t)i + d], a.ulo[parity][4 * (int64_t)i + d]});
+            df_to_double(df{a.rec[parity][8 * (int64_t)i + 4 + d], a.ulo[parity][4 * (int64_t)i + d]});
         if (a.vel && a.ud)
             a.ud[o + d] =
                 df_to_double(df{a.vel[8 * (int64_t)i + d], a.vel[8 * (int64_t)i + 4 + d]});
@@ -111,10 +112,10 @@ __global__ void k_bond_extent(const int32_t* __restrict__ nlist, const double* _
 
 int validate_mixed(const pp_fused_args& a) {
     using mixed::kMaxTable;
-    if (!a.pos_q || !a.uhi[0] || !a.uhi[1] || !a.ulo[0] || !a.ulo[1] || !a.frc || !a.nflags)
+    if (!a.rec[0] || !a.rec[1] || !a.ulo[0] || !a.ulo[1] || !a.frc || !a.nflags)
         return PP_ERROR_INVALID_VALUE;
-    if (!aligned16(a.pos_q) || !aligned16(a.uhi[0]) || !aligned16(a.uhi[1]) ||
-        !aligned16(a.ulo[0]) || !aligned16(a.ulo[1]) || !aligned16(a.frc))
+    if (!aligned32(a.rec[0]) || !aligned32(a.rec[1]) || !aligned16(a.ulo[0]) ||
+        !aligned16(a.ulo[1]) || !aligned16(a.frc))
         return PP_ERROR_MISALIGNED;
     if (a.integrator != PP_EULER && (!a.vel || !a.acc || !a.rho32)) return PP_ERROR_INVALID_VALUE;
     if (a.stiffness_corrections && !a.sc32) return PP_ERROR_INVALID_VALUE;
@@ -123,7 +124,6 @@ int validate_mixed(const pp_fused_args& a) {
     if (a.variant < 0 || a.variant >= PP_MIXED_VARIANTS) return PP_ERROR_INVALID_VALUE;
     if (!a.umax || !a.status) return PP_ERROR_INVALID_VALUE;
     if (a.max_neigh > 256) return PP_ERROR_UNSUPPORTED;
-    if (a.max_neigh >= 64 && !aligned16(a.nlist)) return PP_ERROR_MISALIGNED;  // bulk copies
     if (a.node_instance && a.ninstances > kMaxTable) return PP_ERROR_UNSUPPORTED;
     return PP_SUCCESS;
 }
@@ -162,11 +162,10 @@ extern "C" int pp_mixed_pack(const pp_fused_args* args, int32_t parity, void* st
     const pp_fused_args& a = *args;
     if (a.nnodes < 0 || !is_pow2_le_1024(a.max_neigh)) return PP_ERROR_INVALID_VALUE;
     if (a.nnodes == 0) return PP_SUCCESS;
-    if (!a.r0 || !a.vols || !a.u[parity] || !a.pos_q || !a.uhi[parity] || !a.ulo[parity] ||
-        !a.nflags || !a.bc_types || !a.fc_types || !(a.pos_scale > 0.0))
+    if (!a.r0 || !a.vols || !a.u[parity] || !a.rec[parity] || !a.ulo[parity] || !a.nflags ||
+        !a.bc_types || !a.fc_types || !(a.pos_scale > 0.0))
         return PP_ERROR_INVALID_VALUE;
-    if (!aligned16(a.pos_q) || !aligned16(a.uhi[parity]) || !aligned16(a.ulo[parity]))
-        return PP_ERROR_MISALIGNED;
+    if (!aligned32(a.rec[parity]) || !aligned16(a.ulo[parity])) return PP_ERROR_MISALIGNED;
     if (a.vel && (!a.acc || !a.rho32)) return PP_ERROR_INVALID_VALUE;
     if (a.sc32 && !a.stiffness_corrections) return PP_ERROR_INVALID_VALUE;
     k_mixed_pack<<<(a.nnodes + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, parity);
@@ -178,7 +177,7 @@ extern "C" int pp_mixed_export(const pp_fused_args* args, int32_t parity, void* 
     const pp_fused_args& a = *args;
     if (a.nnodes < 0) return PP_ERROR_INVALID_VALUE;
     if (a.nnodes == 0) return PP_SUCCESS;
-    if (!a.u[parity] || !a.uhi[parity] || !a.ulo[parity] || !a.frc || !a.n_neigh || !a.family)
+    if (!a.u[parity] || !a.rec[parity] || !a.ulo[parity] || !a.frc || !a.n_neigh || !a.family)
         return PP_ERROR_INVALID_VALUE;
     k_mixed_export<<<(a.nnodes + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(a,
                                                                                        parity);

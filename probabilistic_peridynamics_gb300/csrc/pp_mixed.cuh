@@ -1,26 +1,30 @@
 // pp_mixed.cuh -- the PP_MIXED fused step kernel (templates), shared by the
 // translation units that instantiate its tile shapes (pp_mixed_v*.cu).
 //
-// gathers, the break / regime decision taken exactly as binary64 would on
-// the same state, and double-float node state.
+// FP32 bond arithmetic on 32-byte node records gathered with one 256-bit
+// load per bond, the break / regime decision taken exactly as binary64
+// would on the same state, and double-float node state.
 //
-// Structure of one launch (one CTA = 8 warps = 64 consecutive nodes):
+// Structure of one launch (one CTA = W warps, chunks of 8 W consecutive
+// nodes, persistent over the chunks):
 //
-//  1. Bond phase, one warp per node (8 nodes per warp, the CTA's warps
-//     working on 8 consecutive nodes at a time so their neighbourhoods share
-//     L1 lines).  For the lane's max_neigh/32 slots: load all neighbour
-//     indices, then all gathers (int4 fixed-point position + k*vol, float4
-//     displacement + max|u|), then the FP32 bond arithmetic.  A slot whose
-//     FP32 stretch lies within the proven error band of a critical stretch
-//     is deferred to a slow path that evaluates the binary64 stretch of
+//  1. Bond phase, one warp per node (the CTA's warps working on W
+//     consecutive nodes at a time so their neighbourhoods share L1 lines;
+//     no shared-memory staging, so L1 keeps its full capacity for the
+//     records).  Lane l takes slots l, l + 32, ...: the neighbour indices
+//     were loaded while the warp worked on its previous node; then all
+//     record gathers, then the FP32 bond arithmetic.  A slot whose FP32
+//     stretch lies within the proven error band of a critical stretch is
+//     deferred to a slow path that evaluates the binary64 stretch of
 //     peridynamics.cl:65-75 from the reference r0 and the exact
 //     double-float displacement.  The four per-node sums (force x, y, z and
 //     the intact count) are reduced with a 6-shuffle transposed butterfly
 //     and parked in shared memory.
-//  2. Node phase, all 256 threads: thread (node, component) applies the
-//     force boundary condition and the integrator update of one DOF in
-//     double-float arithmetic; every load and store of the node state is a
-//     contiguous 1 KB access per CTA.
+//  2. Node phase, all threads: thread (node, component) applies the force
+//     boundary condition and the integrator update of one DOF in
+//     double-float arithmetic and writes one word of each half of the
+//     node's next record; every load and store of the node state is
+//     contiguous per CTA.
 //
 // Integer-to-float conversion uses the exponent trick
 // float(q) = bits(0x4B400000 + q) - 1.5*2^23 (exact for |q| < 2^22), folded
@@ -33,15 +37,15 @@
 // the binary64 slow path is unaffected by those flags.
 #pragma once
 
+
 #include "pp_bond_f64.cuh"
 #include "pp_fused.cuh"
-#include "pp_tma.cuh"
 
 namespace pp {
 namespace mixed {
 
 constexpr int kMaxTable = 256;
-constexpr int kNodesPerWarp = 8;  // a CTA of W warps owns chunks of 8*W nodes
+constexpr int kNodesPerWarp = 16;  // a CTA of W warps owns chunks of 16*W nodes
 
 constexpr int kMagicI = 0x4B400000;  // bit pattern of 1.5 * 2^23
 constexpr float kMagicF = 12582912.0f;
@@ -65,6 +69,35 @@ struct Bond32 {
     float ry;          // 1 / |p|
     float rxi;         // 1 / |xi|
 };
+
+// One node record {q, w; u, m} (32 bytes, 32-byte aligned) in one 256-bit
+// read-only load: a step never writes the records it reads.
+struct Rec {
+    int4 q;
+    float4 u;
+};
+
+__device__ __forceinline__ Rec load_rec(const float* rec, int64_t i) {
+    float v[8];
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]),
+          "=f"(v[7])
+        : "l"(rec + 8 * i));
+    Rec r;
+    r.q = make_int4(__float_as_int(v[0]), __float_as_int(v[1]), __float_as_int(v[2]),
+                    __float_as_int(v[3]));
+    r.u = make_float4(v[4], v[5], v[6], v[7]);
+    return r;
+}
+
+// Neighbour-list word that the step reads once and may overwrite (-1 on a
+// break) later in the same thread: a coherent load that does not allocate
+// in L1, which is kept for the node records.
+__device__ __forceinline__ int load_slot(const int32_t* p) {
+    int v;
+    asm volatile("ld.global.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
 
 __device__ __forceinline__ float fixed_diff(int qj, int qi, const MixedConst& c) {
     return fmaf(__int_as_float(qj - qi + kMagicI), c.h, c.mh);
@@ -131,8 +164,10 @@ __device__ __forceinline__ QuickBand quick_band(float U, const MixedConst& c) {
 // double-float displacement, in the reference operation order
 // (peridynamics.cl:65-75).
 static __device__ __noinline__ double exact_stretch(const pp_fused_args& a, int parity, int i, int j) {
-    const float4 hi_i = ldg_f4(a.uhi[parity], i), lo_i = ldg_f4(a.ulo[parity], i);
-    const float4 hi_j = ldg_f4(a.uhi[parity], j), lo_j = ldg_f4(a.ulo[parity], j);
+    // the displacement halves of the records (16-byte loads: ptxas 13.0
+    // fails on a 256-bit load inside a non-inlined function)
+    const float4 hi_i = ldg_f4(a.rec[parity], 2 * (int64_t)i + 1), lo_i = ldg_f4(a.ulo[parity], i);
+    const float4 hi_j = ldg_f4(a.rec[parity], 2 * (int64_t)j + 1), lo_j = ldg_f4(a.ulo[parity], j);
     const double* ri = a.r0 + 3 * (int64_t)i;
     const double* rj = a.r0 + 3 * (int64_t)j;
     const double uix = dadd((double)hi_i.x, (double)lo_i.x);
@@ -228,11 +263,8 @@ __device__ __forceinline__ float reduce4c(float x, float cx, float y, float cy, 
     return __fadd_rn(v, vc);
 }
 
-constexpr uint32_t kWaitPolls = 1u << 22;  // bound on mbarrier polls
-
 template <int CH>
 struct alignas(16) MixedShared {
-    uint64_t bar[2];
     float4 frc[CH];
     float thr[kMaxTable], k[kMaxTable], c[kMaxTable];  // regime tables or
                                                         // instance thresholds
@@ -261,19 +293,21 @@ __device__ __forceinline__ Thresholds thresholds(float s0f, float s0err, const Q
 // (force x, y, z, intact count) of local node li in sh.frc[li].  COMP:
 // compensated force sums (acc_mul, reduce4c).
 //
-// A broken or padding slot (-1) gathers node 0 instead of branching around
-// the loads; its arithmetic is discarded (weight 0, not counted).
+// A broken or padding slot (-1) gathers node i itself instead of branching
+// around the loads: its bond vector is exactly 0, so its (discarded, weight
+// 0) contribution stays finite.
 template <int SL, bool CORR, bool TYPES, bool COMP, class Shared>
 __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const MixedConst& c,
                                                 const QuickBand& qb, const Thresholds& th0,
-                                                Shared& sh, const int32_t* nl_row, int parity,
+                                                Shared& sh, const int (&jr)[SL], int parity,
                                                 int i, int li, int lane) {
     const int L = a.max_neigh;
     const int nr = a.nregimes;
     const int64_t row = (int64_t)i * L;
-    const float* __restrict__ uhi = a.uhi[parity];
-    const int4 qi = ldg_i4(a.pos_q, i);
-    const float4 ui = ldg_f4(uhi, i);
+    const float* __restrict__ rec = a.rec[parity];
+    const Rec ri = load_rec(rec, i);
+    const int4 qi = ri.q;
+    const float4 ui = ri.u;
     // critical stretch of this node (per instance when batched)
     float s0f = c.s0, s0err = c.s0_err;
     double s0d = a.critical_stretch;
@@ -286,27 +320,27 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
         th.lo = sh.tlo[inst];
         th.hi = sh.thi[inst];
     }
-    int jr[SL];
-#pragma unroll
-    for (int k = 0; k < SL; ++k) {
-        const int slot = lane + 32 * k;
-        jr[k] = (SL > 1 || slot < L) ? nl_row[slot] : -1;
-    }
+    // this lane's slots: lane + 32 k (consecutive lanes gather consecutive
+    // neighbours of the row)
+    const int64_t g0 = row + lane;
+    int32_t* const nl_g = a.nlist + g0;
     int4 qj[SL];
     float4 uj[SL];
     float sc[SL];
     int bt[SL], rg[SL];
 #pragma unroll
     for (int k = 0; k < SL; ++k) {
-        const int jj = max(jr[k], 0);
-        qj[k] = ldg_i4(a.pos_q, jj);
-        uj[k] = ldg_f4(uhi, jj);
-        const int64_t gid = row + lane + 32 * k;
-        if constexpr (CORR) sc[k] = __ldcs(a.sc32 + gid);
+        if constexpr (CORR) sc[k] = (SL > 1 || lane < L) ? __ldcs(a.sc32 + g0 + 32 * k) : 0.f;
         if constexpr (TYPES) {
-            bt[k] = jr[k] != -1 ? __ldcs(a.bond_types + gid) * nr : 0;
-            rg[k] = jr[k] != -1 ? a.regimes[gid] : 0;
+            bt[k] = jr[k] != -1 ? __ldcs(a.bond_types + g0 + 32 * k) * nr : 0;
+            rg[k] = jr[k] != -1 ? a.regimes[g0 + 32 * k] : 0;
         }
+    }
+#pragma unroll
+    for (int k = 0; k < SL; ++k) {
+        const Rec rj = load_rec(rec, jr[k] < 0 ? i : jr[k]);
+        qj[k] = rj.q;
+        uj[k] = rj.u;
     }
     float sx = 0.f, sy = 0.f, sz = 0.f;
     float cx = 0.f, cy = 0.f, cz = 0.f;  // carries (COMP)
@@ -328,12 +362,11 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
                 else
                     intact = d < 0.0f, broken = !intact;
             }
-            if (valid && broken) a.nlist[row + lane + 32 * k] = -1;
+            if (valid && broken) nl_g[32 * k] = -1;
             intact = intact && valid;
             w *= b.s;
         } else {
             if (!valid) continue;
-            const int64_t gid = row + lane + 32 * k;
             bool ambiguous = false;
             const int reg = next_regime(rg[k], bt[k], nr, [&](int idx) {
                 if (b.s < sh.tlo[idx]) return true;
@@ -348,20 +381,19 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
                 amb |= 1u << k;
                 continue;
             }
-            if (reg != rg[k]) a.regimes[gid] = reg;
+            if (reg != rg[k]) a.regimes[g0 + 32 * k] = reg;
             intact = reg < nr;
             if (!intact) {
-                a.nlist[gid] = -1;
+                nl_g[32 * k] = -1;
                 continue;
             }
             w *= fmaf(b.s, sh.k[bt[k] + reg], sh.c[bt[k] + reg]);
         }
         float fv = intact ? w * b.ry : 0.0f;
         if constexpr (CORR) fv *= sc[k];
-        const float px = intact ? b.px : 0.0f;  // finite for discarded slots
-        acc_mul<COMP>(sx, cx, fv, px);
-        acc_mul<COMP>(sy, cy, fv, intact ? b.py : 0.0f);
-        acc_mul<COMP>(sz, cz, fv, intact ? b.pz : 0.0f);
+        acc_mul<COMP>(sx, cx, fv, b.px);
+        acc_mul<COMP>(sy, cy, fv, b.py);
+        acc_mul<COMP>(sz, cz, fv, b.pz);
         cnt += intact ? 1.0f : 0.0f;
     }
     // Slow path: slots whose FP32 stretch is too close to a critical stretch
@@ -370,10 +402,12 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
 #pragma unroll
         for (int k = 0; k < SL; ++k) {
             if (!((amb >> k) & 1u)) continue;
-            const int64_t gid = row + lane + 32 * k;
-            const Bond32 b = bond32(qi, ui, qj[k], uj[k], c);
+            // gathered again: keeping the first loop's records live until
+            // here would cost the common path their registers
+            const Rec rj = load_rec(rec, jr[k]);
+            const Bond32 b = bond32(qi, ui, rj.q, rj.u, c);
             const double s64 = exact_stretch(a, parity, i, jr[k]);
-            float w = __int_as_float(qj[k].w);
+            float w = __int_as_float(rj.q.w);
             bool intact;
             if constexpr (!TYPES) {
                 intact = s64 < s0d;
@@ -382,12 +416,12 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
                 const int reg = next_regime(rg[k], bt[k], nr, [&](int idx) {
                     return s64 < a.critical_stretch_table[idx];
                 });
-                if (reg != rg[k]) a.regimes[gid] = reg;
+                if (reg != rg[k]) a.regimes[g0 + 32 * k] = reg;
                 intact = reg < nr;
                 if (intact) w *= fmaf(b.s, sh.k[bt[k] + reg], sh.c[bt[k] + reg]);
             }
             if (!intact) {
-                a.nlist[gid] = -1;
+                nl_g[32 * k] = -1;
                 continue;
             }
             float fv = w * b.ry;
@@ -410,8 +444,7 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
 template <class Shared>
 __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedConst& c,
                                            const Shared& sh, const StepMags& m, int parity,
-                                           int node0) {
-    const int li = threadIdx.x >> 2;
+                                           int node0, int li) {
     const int comp = threadIdx.x & 3;
     const int i = node0 + li;
     const bool active = i < a.nnodes;
@@ -424,7 +457,7 @@ __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedCo
         const int64_t o3 = 3 * (int64_t)i + comp;
         float frc = body;
         if ((fl >> (3 + comp)) & 1) frc = (float)((double)body + m.force * a.fc_values[o3]);
-        df uu{a.uhi[parity][o4], a.ulo[parity][o4]};
+        df uu{a.rec[parity][8 * (int64_t)i + 4 + comp], a.ulo[parity][o4]};
         const df dt{c.dt_hi, c.dt_lo};
         if (a.integrator == PP_EULER) {
             uu = df_add(uu, df_mul_f(dt, frc));
@@ -432,15 +465,15 @@ __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedCo
             const df half{c.half_hi, c.half_lo};
             const int64_t o8 = 8 * (int64_t)i + comp;
             df v{a.vel[o8], a.vel[o8 + 4]};
-            const float rho = a.rho32[o4];
+            const float rinv = a.rho32[o4];  // 1 / density
             float acc;
             if (a.integrator == PP_EULER_CROMER) {
-                acc = __fdiv_rn(frc - c.damping * v.hi, rho);
+                acc = (frc - c.damping * v.hi) * rinv;
                 v = df_add(v, df_mul_f(dt, acc));
                 uu = df_add(uu, df_mul(dt, v));
             } else {
                 const df v1 = df_add(v, df_mul_f(half, a.acc[o4]));
-                acc = __fdiv_rn(frc - c.damping * v1.hi, rho);
+                acc = (frc - c.damping * v1.hi) * rinv;
                 v = df_add(v1, df_mul_f(half, acc));
                 uu = df_add(uu, df_mul(dt, df_add(v, df_mul_f(half, acc))));
             }
@@ -460,11 +493,14 @@ __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedCo
     um = fmaxf(um, __shfl_xor_sync(kFull, um, 2));
     um *= 1.0f + 1.2e-7f;
     if (active) {
+        // the whole record: position word comp, displacement word 4 + comp
+        const int64_t o8 = 8 * (int64_t)i + comp;
+        a.rec[parity ^ 1][o8] = a.rec[parity][o8];
         if (comp < 3) {
-            a.uhi[parity ^ 1][o4] = hi_new;
+            a.rec[parity ^ 1][o8 + 4] = hi_new;
             a.ulo[parity ^ 1][o4] = lo_new;
         } else {
-            a.uhi[parity ^ 1][o4] = um;
+            a.rec[parity ^ 1][o8 + 4] = um;
             a.ulo[parity ^ 1][o4] = 0.f;
             a.n_neigh[i] = (int)fr.w;
         }
@@ -474,18 +510,16 @@ __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedCo
     if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(reinterpret_cast<int*>(a.umax), wmax);
 }
 
-// One CTA of W warps loops over chunks of 8*W nodes.  For SL >= 2 the chunk's
-// neighbour-list rows (contiguous) stream into shared memory by bulk copy,
-// double-buffered one chunk ahead; for SL == 1 they are read in place.
+// One CTA of W warps loops over chunks of 16*W consecutive nodes (chunks
+// strided by the grid: a persistent launch).  Warp w takes nodes w, W + w,
+// ... of the chunk, so the CTA's warps work on W consecutive nodes at a time
+// and share their neighbours in L1.  Each warp loads the neighbour indices
+// of its next node while it works on the current one.
 template <int SL, bool CORR, bool TYPES, bool COMP, int W, int MINB>
 __global__ void __launch_bounds__(W * 32, MINB)
     k_mixed(pp_fused_args a, MixedConst c, int parity, Launch l) {
     constexpr int kChunk = kNodesPerWarp * W;
-    using Shared = MixedShared<kChunk>;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    Shared& sh = *reinterpret_cast<Shared*>(smem_raw);
-    int32_t* s_nl = reinterpret_cast<int32_t*>(smem_raw + sizeof(Shared));
-    constexpr bool kBulk = SL >= 2;
+    __shared__ MixedShared<kChunk> sh;
     const int L = a.max_neigh;
     const int nchunks = (a.nnodes + kChunk - 1) / kChunk;
     const int lane = threadIdx.x & 31;
@@ -514,59 +548,35 @@ __global__ void __launch_bounds__(W * 32, MINB)
                 sh.thi[t] = th.hi;
             }
     }
-    uint64_t policy = 0;
-    auto issue = [&](int chunk, int buf) {
-        const int n0 = chunk * kChunk;
-        const int nn = min(kChunk, a.nnodes - n0);
-        const uint32_t bytes = (uint32_t)nn * (uint32_t)L * 4u;
-        mbar_arrive_expect_tx(&sh.bar[buf], bytes);
-        bulk_copy_g2s(s_nl + (size_t)buf * kChunk * L, a.nlist + (int64_t)n0 * L, bytes,
-                      &sh.bar[buf], policy);
-    };
-    if constexpr (kBulk) {
-        if (threadIdx.x == 0) {
-            policy = l2_evict_first_policy();
-            mbar_init(&sh.bar[0], 1);
-            mbar_init(&sh.bar[1], 1);
-            fence_mbar_init();
-        }
-        __syncthreads();
-        if (threadIdx.x == 0 && (int)blockIdx.x < nchunks) issue(blockIdx.x, 0);
-    } else {
-        __syncthreads();
-    }
+    __syncthreads();
     const StepMags m = step_mags(l);
     const Thresholds th0 = thresholds(c.s0, c.s0_err, qb);
-    int it = 0;
-    for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x, ++it) {
-        const int buf = it & 1;
+    const bool has = SL > 1 || lane < L;
+    // neighbour slots of node i (-1 beyond the row or past the last node)
+    auto load_row = [&](int i, int (&jr)[SL]) {
+#pragma unroll
+        for (int k = 0; k < SL; ++k)
+            jr[k] = (i < a.nnodes && has) ? load_slot(a.nlist + (int64_t)i * L + lane + 32 * k)
+                                          : -1;
+    };
+    int jn[SL];
+    load_row(blockIdx.x * kChunk + warp, jn);
+    for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
         const int node0 = chunk * kChunk;
-        if constexpr (kBulk) {
-            const int next = chunk + gridDim.x;
-            if (threadIdx.x == 0 && next < nchunks) issue(next, buf ^ 1);
-            const bool ok = mbar_wait_bounded(&sh.bar[buf], (it >> 1) & 1, kWaitPolls);
-            if (__syncthreads_or(!ok)) {
-                // A copy never completed: report, drain the other buffer's
-                // copy (bounded), and leave without touching the state.
-                if (threadIdx.x == 0) {
-                    atomicExch(a.status, PP_STATUS_COPY_TIMEOUT);
-                    if (next < nchunks)
-                        mbar_wait_bounded(&sh.bar[buf ^ 1], ((it + 1) >> 1) & 1, kWaitPolls);
-                }
-                return;
-            }
-        }
         for (int t = 0; t < kNodesPerWarp; ++t) {
             const int li = t * W + warp;
             const int i = node0 + li;
             if (i >= a.nnodes) break;  // warp-uniform
-            const int32_t* nl_row = kBulk ? s_nl + (size_t)buf * kChunk * L + (size_t)li * L
-                                          : a.nlist + (int64_t)i * L;
-            bond_phase_node<SL, CORR, TYPES, COMP>(a, c, qb, th0, sh, nl_row, parity, i, li,
-                                                   lane);
+            int jr[SL];
+#pragma unroll
+            for (int k = 0; k < SL; ++k) jr[k] = jn[k];
+            const int next = t + 1 < kNodesPerWarp ? i + W : (chunk + gridDim.x) * kChunk + warp;
+            load_row(next, jn);
+            bond_phase_node<SL, CORR, TYPES, COMP>(a, c, qb, th0, sh, jr, parity, i, li, lane);
         }
         __syncthreads();
-        node_phase(a, c, sh, m, parity, node0);
+        for (int li = threadIdx.x >> 2; li < kChunk; li += blockDim.x >> 2)
+            node_phase(a, c, sh, m, parity, node0, li);
         __syncthreads();
     }
 }
@@ -605,25 +615,18 @@ template <int SL, bool CORR, bool TYPES, bool COMP, int W, int MINB>
 int launch_instance(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
     constexpr int kChunk = kNodesPerWarp * W;
     auto kernel = k_mixed<SL, CORR, TYPES, COMP, W, MINB>;
-    const size_t smem = sizeof(MixedShared<kChunk>) +
-                        (SL >= 2 ? 2 * (size_t)kChunk * a.max_neigh * sizeof(int32_t) : 0);
-    static size_t cached_smem = 0;
     static int cached_grid = 0;
-    if (cached_smem != smem) {
-        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess)
-            return PP_ERROR_CUDA;
+    if (cached_grid == 0) {
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, W * 32, smem) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, W * 32, 0) !=
                 cudaSuccess ||
             per_sm < 1)
             return PP_ERROR_CUDA;
         cached_grid = per_sm * sm_count();
-        cached_smem = smem;
     }
     const int nchunks = (a.nnodes + kChunk - 1) / kChunk;
     const int grid = nchunks < cached_grid ? nchunks : cached_grid;
-    kernel<<<grid, W * 32, smem, st>>>(a, mixed_const(a), parity, l);
+    kernel<<<grid, W * 32, 0, st>>>(a, mixed_const(a), parity, l);
     return launch_status();
 }
 

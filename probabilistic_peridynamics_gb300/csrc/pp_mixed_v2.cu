@@ -1,4 +1,4 @@
-// pp_mixed_v2.cu -- PP_MIXED tile shape 2: 4 warps x 32 nodes per CTA, register
+// pp_mixed_v2.cu -- PP_MIXED tile shape 2: 4 warps x 64 nodes per CTA, register
 // budget for 6 resident CTAs per SM (kernel template in pp_mixed.cuh).
 #include "pp_mixed.cuh"
 

@@ -50,10 +50,10 @@ __global__ void k_reset_words(StaticScratch* s) {
 
 // Running max |u| of the state: max over nodes of the gathered max|u|
 // (the .w of each displacement record), as the mixed step maintains it.
-__global__ void k_umax_of_state(const float* __restrict__ uhi, int nnodes, StaticScratch* s) {
+__global__ void k_umax_of_state(const float* __restrict__ rec, int nnodes, StaticScratch* s) {
     float m = 0.0f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnodes; i += gridDim.x * blockDim.x)
-        m = fmaxf(m, uhi[4 * (int64_t)i + 3]);
+        m = fmaxf(m, rec[8 * (int64_t)i + 7]);
     const int w = __reduce_max_sync(kFull, __float_as_int(m));
     if ((threadIdx.x & 31) == 0 && w > 0) atomicMax(reinterpret_cast<int*>(&s->umax), w);
 }
@@ -90,7 +90,7 @@ extern "C" int pp_fused_run_static(const pp_fused_args* args, int32_t parity, in
         return PP_ERROR_CUDA;
     if (a.precision == PP_MIXED) {
         const int blocks = (a.nnodes + 255) / 256 < 1024 ? (a.nnodes + 255) / 256 : 1024;
-        k_umax_of_state<<<blocks, 256, 0, st>>>(a.uhi[parity], a.nnodes, s);
+        k_umax_of_state<<<blocks, 256, 0, st>>>(a.rec[parity], a.nnodes, s);
         if (launch_status() != PP_SUCCESS) return PP_ERROR_CUDA;
     }
     int p = parity;

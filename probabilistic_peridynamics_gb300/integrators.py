@@ -401,8 +401,8 @@ class _CUDAIntegrator(Integrator):
     def _create_mixed_buffers(self):
         torch = self._torch
         n, mn = self.nnodes, self.max_neighbours
-        self.pos_q_d = self._empty((n, 4), torch.int32)
-        self.uhi_d = [self._zeros((n, 4), torch.float32) for _ in range(2)]
+        # 32-byte node records {q, w; u, max|u|} (pp_fused_args.rec)
+        self.rec_d = [self._zeros((n, 8), torch.float32) for _ in range(2)]
         self.ulo_d = [self._zeros((n, 4), torch.float32) for _ in range(2)]
         self.frc_d = self._zeros((n, 8), torch.float32)
         if self._dynamic:
@@ -469,9 +469,8 @@ class _CUDAIntegrator(Integrator):
         a.n_neigh = _ptr(self.n_neigh_d)
         a.damage = _ptr(self.damage_d)
         if self.precision == "mixed":
-            a.pos_q = _ptr(self.pos_q_d)
-            a.uhi[0] = self.uhi_d[0].data_ptr()
-            a.uhi[1] = self.uhi_d[1].data_ptr()
+            a.rec[0] = self.rec_d[0].data_ptr()
+            a.rec[1] = self.rec_d[1].data_ptr()
             a.ulo[0] = self.ulo_d[0].data_ptr()
             a.ulo[1] = self.ulo_d[1].data_ptr()
             a.vel = _ptr(self.vel_d)

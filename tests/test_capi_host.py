@@ -109,8 +109,9 @@ def test_validation_without_gpu(L):
                  "nflags", "umax", "status"):
         setattr(fa, name, base)
     fa.precision = _lib.PP_MIXED
-    fa.pos_q = base + 4
-    fa.uhi[0] = fa.uhi[1] = fa.ulo[0] = fa.ulo[1] = base
+    fa.rec[0] = base + 16  # records must be 32-byte aligned
+    fa.rec[1] = base
+    fa.ulo[0] = fa.ulo[1] = base
     fa.pos_scale = 1.0
     assert L.pp_fused_step(ctypes.byref(fa), 0, 0.0, 0.0, None) == \
         _lib.PP_ERROR_MISALIGNED
