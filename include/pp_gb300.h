@@ -50,10 +50,13 @@ extern "C" {
 /* Number of PP_MIXED kernel variants (pp_fused_args.variant). */
 #define PP_MIXED_VARIANTS           3
 
-/* Values of pp_fused_args.status after a step (read by the caller). */
+/* Values of pp_fused_args.status after a step (read by the caller).  The
+ * word reports errors that a kernel detects on the device; a kernel with a
+ * bounded wait sets PP_STATUS_COPY_TIMEOUT when the wait runs out.  The
+ * PP_MIXED step of this version has no waits and leaves PP_STATUS_OK.     */
 #define PP_STATUS_OK                0
-#define PP_STATUS_COPY_TIMEOUT      1  /* a bulk copy did not complete: the
-                                          step's results are invalid     */
+#define PP_STATUS_COPY_TIMEOUT      1  /* a wait for an asynchronous copy ran
+                                          out: the step's results are invalid */
 
 /* Flags of the fused step. */
 #define PP_FLAG_COMPENSATED         1  /* PP_MIXED only: compensated FP32 force
@@ -240,8 +243,7 @@ typedef struct pp_fused_args {
     float* sc32;
     int32_t* nflags;               /* (nnodes) boundary-condition flags    */
     float* umax;                   /* device word: running max of |u| (scratch) */
-    int32_t* status;               /* device word: 0, or PP_STATUS_* set by a
-                                      kernel that gave up waiting (scratch) */
+    int32_t* status;               /* device word: PP_STATUS_* (scratch)   */
     double pos_scale;
     double min_bond;               /* smallest |xi| over the bonds (pp_bond_extent) */
     double pos_origin[3];

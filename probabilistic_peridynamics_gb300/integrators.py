@@ -606,8 +606,8 @@ class _CUDAIntegrator(Integrator):
             status = int(self.status_d.cpu().item())
             if status != _lib.PP_STATUS_OK:
                 raise _lib.LibraryError(
-                    f"a mixed-precision step reported status {status}: a bulk "
-                    "copy did not complete and the state is invalid")
+                    f"a mixed-precision step reported device status {status} "
+                    "(PP_STATUS_*): the state is invalid")
         cur = self.u_d[self._parity]
 
         def put(host, dev):
