@@ -214,6 +214,21 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ measurements
+def job_time_ms(ms, dist, torch, device):
+    """The job's time: the largest timed region over the ranks."""
+    if dist is None:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, bonds, steps, ms):
+    """Bond-updates/s of the whole job: every rank steps its own replica
+    of ``bonds`` bonds ``steps`` times within ``ms`` milliseconds."""
+    return world * bonds * steps / (ms * 1e-3)
+
+
 def time_steps(integ, steps, warmup, torch, dist=None, rate=PULL_RATE):
     """Device time of exactly ``steps`` fused steps (graph replays)."""
     dm = torch.as_tensor(rate * np.arange(1, warmup + steps + 1),
@@ -359,15 +374,25 @@ def compact(nlist, family):
     return out
 
 
-def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None):
-    """Time the reference CPU step on an nx x 200 x 10 slab of the lattice.
+#: Pseudo-time step of the reference's Euler update on the CPU samples.  The
+#: reference CPU path has no Velocity-Verlet, and its Euler update
+#: u += dt f is stable only for dt below 2 / lambda_max, lambda_max <=
+#: 2 sum_j c vol / |xi_j| ~ 3e14 on this lattice: at larger dt displacements
+#: grow, every bond breaks within a few steps and the sample stops doing
+#: bond work.  At 1e-15 (dt lambda_max ~ 0.3) no bond breaks and each step
+#: does the workload's bond work.
+CPU_DT = 1e-15
+
+
+def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None, ny=NY):
+    """Time the reference CPU step on an nx x ny x 10 block of the lattice.
 
     :returns: (bond-updates/s, steps run, seconds, bonds per step, kind,
-        cores)
+        cores, bonds broken during the sample)
     """
     from probabilistic_peridynamics_gb300 import lattice
-    coords = lattice.lattice_coords(nx, NY, NZ, DX)
-    family, nlist, _ = lattice.lattice_family(nx, NY, NZ, HORIZON_CELLS,
+    coords = lattice.lattice_coords(nx, ny, NZ, DX)
+    family, nlist, _ = lattice.lattice_family(nx, ny, NZ, HORIZON_CELLS,
                                               pow2=False)
     n = coords.shape[0]
     bonds = int(family.sum())
@@ -387,15 +412,21 @@ def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None):
             f = mod.bond_force(coords + u, coords, nl, n_neigh, vol, k, fcv,
                                fct, 0.0)
             mod.update_displacement(u, bc_values, bc_types, f,
-                                    PULL_RATE * s, DT)
+                                    PULL_RATE * s, CPU_DT)
+
+        def intact():
+            return int(n_neigh.sum())
         kind, cores = "reference", 1
     else:
         from oracle import cref
-        st = cref.Stepper("euler", DT, coords, vol, family, nlist, bc_types,
-                          bc_values, fct, fcv, k, S0)
+        st = cref.Stepper("euler", CPU_DT, coords, vol, family, nlist,
+                          bc_types, bc_values, fct, fcv, k, S0)
 
         def step(s):
             st.step(PULL_RATE * s, 0.0)
+
+        def intact():
+            return int((st.nlist != -1).sum())
         kind, cores = "port", os.cpu_count() or 1
     t0 = time.perf_counter()
     done = 0
@@ -409,18 +440,19 @@ def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None):
         elif done >= max_steps or (el >= budget_s and done >= min_steps):
             break
     el = time.perf_counter() - t0
-    return bonds * done / el, done, el, bonds, kind, cores
+    return bonds * done / el, done, el, bonds, kind, cores, bonds - intact()
 
 
 def cpu_baseline():
-    rate, steps, el, bonds, kind, cores = cpu_sample(NX, budget_s=10.0)
+    rate, steps, el, bonds, kind, cores, broken = cpu_sample(NX,
+                                                             budget_s=10.0)
     what = ("reference Cython Euler step (peripy/peridynamics.pyx break_bonds"
             " + bond_force + update_displacement)" if kind == "reference"
             else "C restatement of the OpenCL step (OpenMP)")
     return {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
             "sample": f"{steps} step(s) of the {what} on the full "
-                      f"{NX}x{NY}x{NZ} lattice ({bonds} bonds/step), "
-                      f"{el:.1f} s"}
+                      f"{NX}x{NY}x{NZ} lattice ({bonds} bonds/step, Euler "
+                      f"dt {CPU_DT:g}, {broken} bonds broken), {el:.1f} s"}
 
 
 def reference_arm(args):
@@ -428,20 +460,25 @@ def reference_arm(args):
     if rank != 0:
         return
     total = args.steps + args.warmup
-    # Size the slab so that warm-up + timed steps take about 90 s.
+    # Size the block (4 x ny x 10 of the lattice) so that warm-up + timed
+    # steps take about 90 s on one core.
     probe_rate, *_ = cpu_sample(4, budget_s=0.5, min_steps=1, max_steps=3)
     per_step_bonds = probe_rate * 90.0 / max(total, 1)
-    bonds_per_x = 42700528 / NX
-    nx = int(max(4, min(NX, per_step_bonds // bonds_per_x)))
-    from probabilistic_peridynamics_gb300 import lattice  # noqa: F401
+    bonds_4xNY = 4 * NY * NZ * 107.0  # about 107 bonds per node in bulk
+    nx, ny = 4, int(max(4, min(NY, NY * per_step_bonds / bonds_4xNY)))
+    if per_step_bonds > bonds_4xNY:
+        nx = int(max(4, min(NX, 4 * per_step_bonds / bonds_4xNY)))
+        ny = NY
     if args.warmup:
-        cpu_sample(nx, 0.0, steps=args.warmup)
-    rate, steps, el, bonds, kind, cores = cpu_sample(nx, 0.0,
-                                                     steps=args.steps)
-    sample = (f"each step: the reference CPU step on a {nx}x{NY}x{NZ} slab "
-              f"of the lattice ({bonds} bonds)" if kind == "reference" else
-              f"each step: C restatement of the OpenCL step on a "
-              f"{nx}x{NY}x{NZ} slab ({bonds} bonds)")
+        cpu_sample(nx, 0.0, steps=args.warmup, ny=ny)
+    rate, steps, el, bonds, kind, cores, broken = cpu_sample(
+        nx, 0.0, steps=args.steps, ny=ny)
+    what = ("the reference CPU step (Cython break_bonds + bond_force + "
+            "update_displacement)" if kind == "reference" else
+            "C restatement of the OpenCL step")
+    sample = (f"each step: {what} on a {nx}x{ny}x{NZ} block of the lattice "
+              f"({bonds} bonds, Euler dt {CPU_DT:g}, {broken} bonds broken "
+              f"over the run)")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -651,12 +688,9 @@ def main():
     clocks.start()
     ms = time_steps(integ, args.steps, args.warmup, torch, dist)
     clk = clocks.stop()
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = job_time_ms(ms, dist, torch, "cuda")
     ms_per_step = ms / args.steps
-    value = world * w["bonds"] * args.steps / (ms * 1e-3)
+    value = job_throughput(world, w["bonds"], args.steps, ms)
     kernel_ms = time_kernel_launches(integ, 200, torch)
     tuning = integ.tuning
     variant = int(integ._fargs.variant)
