@@ -353,17 +353,11 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
         float w = __int_as_float(qj[k].w);  // k*vol (PMB) or vol (types)
         bool intact;
         if constexpr (!TYPES) {
-            intact = b.s < th.lo;
-            bool broken = b.s > th.hi;
-            if (valid && !intact && !broken) {  // near s0: the bond's own band
-                const float d = b.s - s0f;
-                if (!(fabsf(d) > band32(ui, uj[k], b, c) + s0err))
-                    amb |= 1u << k;  // decided on the binary64 stretch below
-                else
-                    intact = d < 0.0f, broken = !intact;
-            }
-            if (valid && broken) nl_g[32 * k] = -1;
-            intact = intact && valid;
+            // clearly intact below th.lo; every other bond (clearly broken
+            // above th.hi, or between: own band, then binary64) is decided
+            // in the slow path below, where breaks are written
+            intact = valid && b.s < th.lo;
+            if (valid && !intact) amb |= 1u << k;
             w *= b.s;
         } else {
             if (!valid) continue;
@@ -396,8 +390,8 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
         acc_mul<COMP>(sz, cz, fv, b.pz);
         cnt += intact ? 1.0f : 0.0f;
     }
-    // Slow path: slots whose FP32 stretch is too close to a critical stretch
-    // are decided on the binary64 stretch.
+    // Slow path: slots that break, or whose FP32 stretch is too close to a
+    // critical stretch (decided on the binary64 stretch).
     if (__any_sync(kFull, amb != 0u)) {
 #pragma unroll
         for (int k = 0; k < SL; ++k) {
@@ -406,13 +400,21 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
             // here would cost the common path their registers
             const Rec rj = load_rec(rec, jr[k]);
             const Bond32 b = bond32(qi, ui, rj.q, rj.u, c);
-            const double s64 = exact_stretch(a, parity, i, jr[k]);
             float w = __int_as_float(rj.q.w);
             bool intact;
             if constexpr (!TYPES) {
-                intact = s64 < s0d;
+                // clearly broken, or the bond's own error band decides;
+                // else binary64
+                const float d = b.s - s0f;
+                if (b.s > th.hi)
+                    intact = false;
+                else if (fabsf(d) > band32(ui, rj.u, b, c) + s0err)
+                    intact = d < 0.0f;
+                else
+                    intact = exact_stretch(a, parity, i, jr[k]) < s0d;
                 w *= b.s;
             } else {
+                const double s64 = exact_stretch(a, parity, i, jr[k]);
                 const int reg = next_regime(rg[k], bt[k], nr, [&](int idx) {
                     return s64 < a.critical_stretch_table[idx];
                 });
