@@ -403,6 +403,9 @@ def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None, ny=NY):
     fcv = np.zeros((n, 3))
     u = np.zeros((n, 3))
     n_neigh = family.copy()
+    # the same strain rate as the full plate: a block nx cells wide is
+    # pulled (nx - 1)/(NX - 1) as fast
+    rate = PULL_RATE * (nx - 1) / (NX - 1)
     mod = reference_step_fn()
     if mod is not None:
         nl = compact(nlist, family)
@@ -411,8 +414,8 @@ def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None, ny=NY):
             mod.break_bonds(coords + u, coords, nl, n_neigh, S0)
             f = mod.bond_force(coords + u, coords, nl, n_neigh, vol, k, fcv,
                                fct, 0.0)
-            mod.update_displacement(u, bc_values, bc_types, f,
-                                    PULL_RATE * s, CPU_DT)
+            mod.update_displacement(u, bc_values, bc_types, f, rate * s,
+                                    CPU_DT)
 
         def intact():
             return int(n_neigh.sum())
@@ -423,7 +426,7 @@ def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None, ny=NY):
                           bc_types, bc_values, fct, fcv, k, S0)
 
         def step(s):
-            st.step(PULL_RATE * s, 0.0)
+            st.step(rate * s, 0.0)
 
         def intact():
             return int((st.nlist != -1).sum())
