@@ -452,13 +452,20 @@ __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedCo
     const bool active = i < a.nnodes;
     const float4 fr = sh.frc[li];
     const int64_t o4 = 4 * (int64_t)i + comp;
+    const int64_t o3 = 3 * (int64_t)i + comp;
+    const int fl = active ? a.nflags[i] : 0;
+    const bool dof = active && comp < 3;
+    // Boundary conditions are binary64 (slow on GB300's FP64 pipe): taken
+    // only by warps that hold a boundary DOF.
+    const bool fbc = dof && ((fl >> (3 + comp)) & 1);
+    const bool dbc = dof && ((fl >> comp) & 1);
+    const bool any_fbc = __any_sync(kFull, fbc);
+    const bool any_dbc = __any_sync(kFull, dbc);
     float hi_new = 0.f, lo_new = 0.f;
-    if (active && comp < 3) {
+    if (dof) {
         const float body = comp == 0 ? fr.x : (comp == 1 ? fr.y : fr.z);
-        const int fl = a.nflags[i];
-        const int64_t o3 = 3 * (int64_t)i + comp;
         float frc = body;
-        if ((fl >> (3 + comp)) & 1) frc = (float)((double)body + m.force * a.fc_values[o3]);
+        if (any_fbc && fbc) frc = (float)((double)body + m.force * a.fc_values[o3]);
         df uu{a.rec[parity][8 * (int64_t)i + 4 + comp], a.ulo[parity][o4]};
         const df dt{c.dt_hi, c.dt_lo};
         if (a.integrator == PP_EULER) {
@@ -483,7 +490,7 @@ __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedCo
             a.vel[o8 + 4] = v.lo;
             a.acc[o4] = acc;
         }
-        if (fl & (1 << comp)) uu = df_from_double(m.disp * a.bc_values[o3]);
+        if (any_dbc && dbc) uu = df_from_double(m.disp * a.bc_values[o3]);
         hi_new = uu.hi;
         lo_new = uu.lo;
         a.frc[8 * (int64_t)i + comp] = frc;
