@@ -570,17 +570,37 @@ def composite_main(args):
     trilinear damage (0.004, 0.006, 0.01), Velocity-Verlet with density
     2400, damping 2.5e6, dt 1e-6, x faces pulled 5e-7 per step; mixed step
     with compensated force sums, its error against the FP64 step after
-    ``--accuracy-steps`` steps with and without compensation."""
+    ``--accuracy-steps`` steps with and without compensation, beside the
+    error of an FP64 run whose initial velocities are perturbed by
+    3e-12 m/s (through fracture the problem amplifies any perturbation)."""
     import torch
     import probabilistic_peridynamics_gb300 as pp
     from probabilistic_peridynamics_gb300.pointset import composite
+    from probabilistic_peridynamics_gb300.integrators import CUDAContext
+    from probabilistic_peridynamics_gb300.model import (build_family,
+                                                        neighbour_pairs)
+    from probabilistic_peridynamics_gb300.neighbours import neighbour_family
+    ctx = CUDAContext(0)
     t0 = time.perf_counter()
-    w = composite()
+    w = composite(context=ctx)
     setup_s = time.perf_counter() - t0
     n = w["coords"].shape[0]
     bonds = int(w["family"].sum())
+    # neighbour families of the 1M points: GPU cell search vs host KD-tree
+    neighbour_family(w["coords"], w["horizon"], ctx)  # warm
+    t0 = time.perf_counter()
+    fam_g, nl_g, _ = neighbour_family(w["coords"], w["horizon"], ctx)
+    gpu_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    fam_h, nl_h, _ = build_family(n, neighbour_pairs(w["coords"],
+                                                     w["horizon"]))
+    host_s = time.perf_counter() - t0
+    neighbours = {"gpu_s": gpu_s, "host_kdtree_s": host_s,
+                  "identical": bool(np.array_equal(fam_g, fam_h) and
+                                    np.array_equal(nl_g, nl_h))}
+    del nl_g, nl_h
 
-    def make(precision, compensated=False):
+    def make(precision, compensated=False, ud0=None):
         integ = pp.VelocityVerletCUDA(DAMPING, dt=DT, precision=precision,
                                       compensated=compensated)
         integ.build(n, 3, w["max_neigh"], w["coords"], w["volume"],
@@ -589,9 +609,9 @@ def composite_main(args):
                     w["bond_types"], w["densities"])
         z = np.zeros((n, 3))
         integ.create_buffers(w["nlist"], w["n_neigh"], w["bond_stiffness"],
-                             w["critical_stretch"], w["plus_cs"], z, z, z, z,
-                             z, np.zeros(n), None, w["nregimes"],
-                             w["nbond_types"])
+                             w["critical_stretch"], w["plus_cs"], z,
+                             z if ud0 is None else ud0, z, z, z, np.zeros(n),
+                             None, w["nregimes"], w["nbond_types"])
         return integ
 
     integ = make("mixed", compensated=True)
@@ -609,10 +629,15 @@ def composite_main(args):
         steps = args.accuracy_steps
         mags = COMPOSITE_RATE * np.arange(1, steps + 1)
         res = {}
-        for name, prec, comp in (("fp64", "float64", False),
-                                 ("mixed", "mixed", False),
-                                 ("mixed_compensated", "mixed", True)):
-            it = make(prec, comp)
+        # the FP64 run from initial velocities perturbed by 3e-12 m/s shows
+        # how far the problem itself carries a perturbation
+        pert = 3e-12 * np.random.default_rng(0).standard_normal((n, 3))
+        for name, prec, comp, ud0 in (
+                ("fp64", "float64", False, None),
+                ("fp64_perturbed", "float64", False, pert),
+                ("mixed", "mixed", False, None),
+                ("mixed_compensated", "mixed", True, None)):
+            it = make(prec, comp, ud0)
             it._run(mags, np.zeros(steps), 0, steps)
             z = [np.zeros((n, 3)) for _ in range(5)]
             res[name] = it.write(*z, np.zeros(n), w["nlist"].copy(),
@@ -624,12 +649,14 @@ def composite_main(args):
                "bonds_broken_fp64": int((w["nlist"] != -1).sum() -
                                         (nl64 != -1).sum()),
                "max_abs_u": float(np.abs(u64).max())}
-        for name in ("mixed", "mixed_compensated"):
+        for name in ("fp64_perturbed", "mixed", "mixed_compensated"):
             u = res[name][0]
             acc[name] = {
                 "disp_rel_err_vs_fp64": float(np.abs(u - u64).max() /
                                               np.abs(u64).max()),
-                "mask_flips_vs_fp64": int((res[name][6] != nl64).sum())}
+                "mask_flips_vs_fp64": int((res[name][6] != nl64).sum()),
+                "bonds_broken": int((w["nlist"] != -1).sum() -
+                                    (res[name][6] != -1).sum())}
     peaks = load_peaks()
     peak = float(peaks["hbm_gbs"]) if peaks else 6800.0
     # int32 nlist + bond_types + regimes per bond; VV node bytes
@@ -645,7 +672,8 @@ def composite_main(args):
                                "in 2.0x1.0x0.1, 3 bond types, trilinear "
                                "damage, Velocity-Verlet",
                    "nodes": n, "bonds": bonds, "max_neigh": w["max_neigh"],
-                   "setup_s": setup_s, "pull_rate": COMPOSITE_RATE,
+                   "setup_s": setup_s, "neighbour_build": neighbours,
+                   "pull_rate": COMPOSITE_RATE,
                    "precision": "mixed, compensated force sums",
                    "tile_shape_autotune_ms": tuning, "variant": variant},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,

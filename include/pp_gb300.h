@@ -288,6 +288,32 @@ int pp_mixed_pack(const pp_fused_args* args, int32_t parity, void* stream);
 int pp_mixed_export(const pp_fused_args* args, int32_t parity, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Neighbour families (set-up).  Replace the host KD-tree search of         */
+/* Model._set_neighbour_list (peripy/model.py:536-597, sklearn KDTree       */
+/* query_radius, rows padded to the CL layout at :575-585).  Two calls on   */
+/* a grid of dims[0] x dims[1] x dims[2] cubic cells of edge `cell` from    */
+/* the corner `lo` (host arrays of 3), covering every node, with            */
+/* cell > horizon * (1 + 1e-9):                                            */
+/*   pp_neighbour_cells bins the nodes: cell_start (ncells + 1 ints) and    */
+/*   order (nnodes ints), device arrays the caller allocates;              */
+/*   pp_neighbour_rows writes family (nnodes ints, the neighbour count of   */
+/*   every node), and, when nlist is not NULL, the (nnodes, max_neigh)      */
+/*   neighbour list: each row in ascending node order, padded with -1;      */
+/*   rows longer than max_neigh are truncated and set *overflow (a device   */
+/*   word) to 1.  Call it once with nlist = NULL to size max_neigh.         */
+/* j is a neighbour of i != j when (dx*dx + dy*dy) + dz*dz <= horizon^2 in   */
+/* binary64 (coords (nnodes, 3) f64 row-major on the device).               */
+/* ------------------------------------------------------------------------ */
+
+int pp_neighbour_cells(const double* coords, int32_t nnodes, const double* lo, double cell,
+                       const int32_t* dims, int32_t* cell_start, int32_t* order, void* stream);
+
+int pp_neighbour_rows(const double* coords, int32_t nnodes, double horizon, const double* lo,
+                      double cell, const int32_t* dims, const int32_t* cell_start,
+                      const int32_t* order, int32_t max_neigh, int32_t* nlist,
+                      int32_t* family, int32_t* overflow, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Adjoint of the Euler step (gradients of a displacement loss).            */
 /* No counterpart in the reference: PeriPy has no gradients.  The forward  */
 /* step is pp_fused_step with PP_FLOAT64, PP_EULER, stiffness corrections   */

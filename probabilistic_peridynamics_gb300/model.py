@@ -7,7 +7,9 @@ all outside the time step:
 
 * meshes are read with the legacy-VTK reader of :mod:`.mesh` (meshio is not
   a dependency; ``.msh`` files are not read);
-* the neighbour search uses ``scipy.spatial.cKDTree.query_pairs`` instead of
+* the neighbour search runs on the GPU for CUDA integrators
+  (:mod:`.neighbours`: a cell grid, one warp per node) and with
+  ``scipy.spatial.cKDTree.query_pairs`` otherwise, instead of
   ``sklearn.neighbors.KDTree.query_radius`` (``model.py:564-566``); the
   neighbour *sets* are the same (distance <= horizon), rows are in
   ascending node order;
@@ -327,10 +329,20 @@ class Model(object):
 
     def _set_neighbour_list(self, coords, horizon, nnodes,
                             initial_crack=None, context=None):
-        """Family, neighbour list and crack (``peripy/model.py:536-597``)."""
-        pairs = neighbour_pairs(coords, horizon)
-        family, nlist, max_neighbours = build_family(
-            nnodes, pairs, pow2=bool(context))
+        """Family, neighbour list and crack (``peripy/model.py:536-597``).
+
+        With a CUDA integrator the families are built on its GPU
+        (:func:`.neighbours.neighbour_family`), else on the host; both give
+        the same rows.
+        """
+        if context:
+            from .neighbours import neighbour_family
+            family, nlist, max_neighbours = neighbour_family(
+                coords, horizon, context, pow2=True)
+        else:
+            pairs = neighbour_pairs(coords, horizon)
+            family, nlist, max_neighbours = build_family(
+                nnodes, pairs, pow2=False)
         n_neigh = family.copy()
         if initial_crack is not None:
             if callable(initial_crack):

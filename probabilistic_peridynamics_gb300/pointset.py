@@ -107,7 +107,8 @@ def trilinear(c, s0, s1, sc):
 
 def composite(count=1_000_000, box=(2.0, 1.0, 0.1), spacing=0.004,
               horizon_factor=3.0, split=1.0, bulk_moduli=(1e9, 3e9),
-              stretches=(0.004, 0.006, 0.01), density=2400.0, seed=5):
+              stretches=(0.004, 0.006, 0.01), density=2400.0, seed=5,
+              context=None):
     """The irregular composite plate: ``count`` Poisson-disk points in
     ``box``, horizon ``horizon_factor * spacing``, node volume box/count.
 
@@ -116,7 +117,8 @@ def composite(count=1_000_000, box=(2.0, 1.0, 0.1), spacing=0.004,
     (``bulk_moduli[1]``), 2 across the interface (micro-modulus the
     harmonic mean of the two).  Every type has the trilinear damage of
     :func:`trilinear` with ``stretches``.  The faces x < horizon and
-    x > box_x - horizon carry displacement BCs -1 and +1 along x.
+    x > box_x - horizon carry displacement BCs -1 and +1 along x.  With a
+    :class:`~.integrators.CUDAContext` the families are built on its GPU.
 
     :returns: dict of the arrays ``Integrator.build``/``create_buffers``
         take (``coords``, ``volume``, ``family``, ``nlist``, ``n_neigh``,
@@ -127,8 +129,12 @@ def composite(count=1_000_000, box=(2.0, 1.0, 0.1), spacing=0.004,
     horizon = horizon_factor * spacing
     coords = poisson_disk((0.0, 0.0, 0.0), box, spacing, count, seed)
     n = coords.shape[0]
-    pairs = neighbour_pairs(coords, horizon)
-    family, nlist, max_neigh = build_family(n, pairs)
+    if context is not None:
+        from .neighbours import neighbour_family
+        family, nlist, max_neigh = neighbour_family(coords, horizon, context)
+    else:
+        family, nlist, max_neigh = build_family(
+            n, neighbour_pairs(coords, horizon))
     valid = nlist != -1
     j = np.where(valid, nlist, 0)
     left_i = coords[:, 0] < split
