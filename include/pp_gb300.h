@@ -314,6 +314,46 @@ int pp_neighbour_rows(const double* coords, int32_t nnodes, double horizon, cons
                       int32_t* family, int32_t* overflow, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Stiffness correction factors (set-up).  Replaces the correction          */
+/* algorithms of peripy/correction.pyx:5-277 as Model.__init__ applies them */
+/* (peripy/model.py:349-375, 782-935): each selected factor multiplies the  */
+/* (nnodes, max_neigh) f64 array `corrections` in place, in the order       */
+/* micromodulus, volume, surface.  Rows hold their n_neigh[i] bonds first   */
+/* (no repeated neighbour); other slots are left as they are.              */
+/*   micromodulus_function 0: conical, (h - l0)/h within h = micromodulus_  */
+/*     horizon; -1: none                                                    */
+/*   volume_correction 0: partial volume, 1 for l0 <= H - R, (H + R - l0) / */
+/*     (2 R) up to H + R, else 0, with H = vc_horizon, R = vc_node_radius;  */
+/*     -1: none                                                            */
+/*   surface_correction 1: 2 family_volume_bulk / (V_i + V_j) with V the    */
+/*     summed volumes of a node's bonds; 0: the same with V = n_neigh *     */
+/*     average_volume; -1: none.  family_volume: (nnodes) f64 scratch.      */
+/* l0 = |r0[j] - r0[i]| in binary64.                                        */
+/* ------------------------------------------------------------------------ */
+
+typedef struct pp_corrections_args {
+    int32_t nnodes;
+    int32_t max_neigh;
+    int32_t micromodulus_function;
+    int32_t volume_correction;
+    int32_t surface_correction;
+    int32_t reserved;              /* must be 0                            */
+    double micromodulus_horizon;
+    double vc_horizon;
+    double vc_node_radius;
+    double family_volume_bulk;
+    double average_volume;
+    const double* r0;              /* (nnodes, 3)                          */
+    const double* volume;          /* (nnodes)                             */
+    const int32_t* nlist;          /* (nnodes, max_neigh)                  */
+    const int32_t* n_neigh;        /* (nnodes)                             */
+    double* corrections;           /* (nnodes, max_neigh), in/out          */
+    double* family_volume;         /* (nnodes) scratch (surface correction) */
+} pp_corrections_args;
+
+int pp_stiffness_corrections(const pp_corrections_args* args, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Adjoint of the Euler step (gradients of a displacement loss).            */
 /* No counterpart in the reference: PeriPy has no gradients.  The forward  */
 /* step is pp_fused_step with PP_FLOAT64, PP_EULER, stiffness corrections   */

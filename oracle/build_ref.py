@@ -4,13 +4,18 @@ INFRASTRUCTURE: the checker and the timed CPU baseline, never the product).
 Recipe
 ------
 1. Where the reference checkout exists (``/root/reference``, read-only),
-   Cython translates ``peripy/peridynamics.pyx`` and ``peripy/spatial.pyx``
-   (which ``peridynamics.pyx`` cimports through ``spatial.pxd``) from where
-   they lie into C files under ``oracle/_ref/src/``.  Nothing is written
+   Cython translates ``peripy/peridynamics.pyx``, ``peripy/correction.pyx``
+   and ``peripy/spatial.pyx`` (which the other two cimport through
+   ``spatial.pxd``) from where they lie into C files under
+   ``oracle/_ref/src/``.  Nothing is written
    into the reference tree and no reference source is copied.
 2. gcc compiles each C file with the reference's own flags (``-O3``,
-   ``setup.py:12``) into ``oracle/_ref/peripy/<module>.so``, importable as
-   ``peripy.peridynamics`` / ``peripy.spatial`` once ``oracle/_ref`` is on
+   ``setup.py:12``) plus ``-ffp-contract=off``, so that binary64 operations
+   round one by one as written on every host (aarch64 gcc would otherwise
+   fuse multiply-adds that the x86-64 build does not), into
+   ``oracle/_ref/peripy/<module>.so``, importable as
+   ``peripy.peridynamics`` / ``peripy.correction`` / ``peripy.spatial`` once
+   ``oracle/_ref`` is on
    ``sys.path`` (``oracle/_ref/peripy/__init__.py`` is an empty file written
    here so the package imports without the reference's own ``__init__``).
 
@@ -29,7 +34,7 @@ HERE = pathlib.Path(__file__).resolve().parent
 REF_OUT = HERE / "_ref"
 SRC = REF_OUT / "src"
 PKG = REF_OUT / "peripy"
-MODULES = ("spatial", "peridynamics")
+MODULES = ("spatial", "peridynamics", "correction")
 DEFAULT_REFERENCE = pathlib.Path("/root/reference")
 
 
@@ -60,8 +65,8 @@ def _compile(quiet):
         out = PKG / f"{name}{_ext_suffix()}"
         if out.exists() and out.stat().st_mtime >= src.stat().st_mtime:
             continue
-        cmd = [cc, "-O3", "-shared", "-fPIC", "-I", include, str(src), "-o",
-               str(out)]
+        cmd = [cc, "-O3", "-ffp-contract=off", "-shared", "-fPIC", "-I",
+               include, str(src), "-o", str(out)]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"compiling {src.name} failed:\n{res.stderr}")
@@ -102,15 +107,15 @@ def build(reference=None, quiet=False):
     return available()
 
 
-def load():
-    """Import and return the compiled ``peripy.peridynamics`` module."""
+def load(module="peridynamics"):
+    """Import and return a compiled reference module (``peripy.<module>``)."""
     if not available():
         raise ImportError("oracle/_ref is not built")
     path = str(REF_OUT)
     if path not in sys.path:
         sys.path.insert(0, path)
     import importlib
-    return importlib.import_module("peripy.peridynamics")
+    return importlib.import_module(f"peripy.{module}")
 
 
 if __name__ == "__main__":

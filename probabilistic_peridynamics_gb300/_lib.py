@@ -82,6 +82,20 @@ class FusedArgs(ctypes.Structure):
     ]
 
 
+class CorrectionsArgs(ctypes.Structure):
+    """Mirror of ``pp_corrections_args``."""
+    _fields_ = [
+        ("nnodes", _i32), ("max_neigh", _i32),
+        ("micromodulus_function", _i32), ("volume_correction", _i32),
+        ("surface_correction", _i32), ("reserved", _i32),
+        ("micromodulus_horizon", _f64), ("vc_horizon", _f64),
+        ("vc_node_radius", _f64), ("family_volume_bulk", _f64),
+        ("average_volume", _f64),
+        ("r0", _vp), ("volume", _vp), ("nlist", _vp), ("n_neigh", _vp),
+        ("corrections", _vp), ("family_volume", _vp),
+    ]
+
+
 class AdjointArgs(ctypes.Structure):
     """Mirror of ``pp_adjoint_args``."""
 
@@ -113,6 +127,8 @@ SIGNATURES = {
         [ctypes.POINTER(FusedArgs), _i32, _i64, _vp, _vp, _i64, _i32, _i32,
          _vp, _vp]),
     "pp_bond_extent": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
+    "pp_stiffness_corrections": (ctypes.c_int,
+                                 [ctypes.POINTER(CorrectionsArgs), _vp]),
     "pp_neighbour_cells": (ctypes.c_int, [_vp, _i32, _vp, _f64, _vp, _vp, _vp,
                                           _vp]),
     "pp_neighbour_rows": (ctypes.c_int, [_vp, _i32, _f64, _vp, _f64, _vp, _vp,

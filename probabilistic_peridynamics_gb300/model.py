@@ -14,8 +14,8 @@ all outside the time step:
   neighbour *sets* are the same (distance <= horizon), rows are in
   ascending node order;
 * ``write_path`` caches arrays as ``.npy`` files instead of HDF5;
-* the stiffness-correction algorithms (``correction.pyx``) are not built;
-  precomputed ``stiffness_corrections`` arrays are accepted.
+* the stiffness-correction algorithms (``correction.pyx``) run on the GPU
+  of the CUDA integrator (:mod:`.corrections`).
 """
 from collections import namedtuple
 import pathlib
@@ -225,14 +225,28 @@ class Model(object):
         self.degrees_freedom = 3
 
         if stiffness_corrections is None:
-            if (micromodulus_function is not None
-                    or volume_correction is not None
-                    or surface_correction is not None):
+            # micromodulus, volume and surface factors
+            # (peripy/model.py:349-375), computed on the integrator's GPU
+            if ((micromodulus_function is not None
+                 or volume_correction is not None
+                 or surface_correction is not None)
+                    and not integrator.context):
                 raise NotImplementedError(
-                    "micromodulus_function, volume_correction and "
-                    "surface_correction are not computed by this package; "
-                    "pass precomputed factors as stiffness_corrections")
-            self.stiffness_corrections = None
+                    "stiffness corrections are computed on the GPU of a "
+                    "CUDA integrator")
+            from .corrections import stiffness_corrections as _corrections
+            self.stiffness_corrections = _corrections(
+                self.coords, self.volume, nlist, n_neigh, horizon,
+                micromodulus_function=micromodulus_function,
+                volume_correction=volume_correction,
+                surface_correction=surface_correction,
+                node_radius=node_radius, dimensions=self.dimensions,
+                search_horizon=self.horizon,
+                context=integrator.context if integrator.context else None)
+            if (self.stiffness_corrections is not None
+                    and self.write_path is not None):
+                write_array(self.write_path, "stiffness_corrections",
+                            self.stiffness_corrections)
         elif type(stiffness_corrections) == np.ndarray:
             if np.shape(stiffness_corrections) != (
                     self.nnodes, self.max_neighbours):

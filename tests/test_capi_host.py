@@ -60,6 +60,9 @@ def test_struct_layout_matches_header():
     assert f["dt"].offset == 40
     assert f["bond_stiffness_table"].offset == 72
     assert f["pos_origin"].offset + 24 == ctypes.sizeof(_lib.FusedArgs)
+    # pp_corrections_args: 6 int32, 5 doubles, 6 pointers
+    assert ctypes.sizeof(_lib.CorrectionsArgs) == 6 * 4 + 5 * 8 + 6 * 8
+    assert _lib.CorrectionsArgs.r0.offset == 64
 
 
 def test_validation_without_gpu(L):
