@@ -1,4 +1,4 @@
-"""Minimal legacy-VTK mesh reader and writer.
+"""Minimal legacy-VTK mesh reader and writer, and a Gmsh MSH 2.x reader.
 
 PeriPy reads meshes with meshio (``peripy/model.py:481-503``) and writes
 them with ``meshio.write_points_cells`` (``peripy/model.py:505-534``).
@@ -162,3 +162,78 @@ def write_vtk(filename, points, cells=(), point_data=None, binary=True):
             put_line(f"{name} {arr.shape[1]} {n} double")
             put_values(arr.ravel(), "double")
     pathlib.Path(filename).write_bytes(bytes(out))
+
+
+#: Gmsh element types (MSH 2) and their node counts, named as meshio names
+#: them in cells_dict.
+MSH_ELEMENTS = {1: ("line", 2), 2: ("triangle", 3), 3: ("quad", 4),
+                4: ("tetra", 4), 5: ("hexahedron", 8), 6: ("wedge", 6),
+                7: ("pyramid", 5), 8: ("line3", 3), 9: ("triangle6", 6),
+                11: ("tetra10", 10), 15: ("vertex", 1)}
+
+
+def read_msh(filename):
+    """Read a Gmsh ASCII MSH 2.x mesh (the format of PeriPy's ``.msh``
+    examples, which it reads with meshio).
+
+    Node coordinates come in file order; element node ids are mapped to
+    those positions.  Elements are grouped by type in file order, as
+    meshio's ``cells_dict`` groups them.
+
+    :returns: :class:`Mesh`.
+    :raises MeshFormatError: for binary or MSH 4 files and unknown element
+        types.
+    """
+    lines = pathlib.Path(filename).read_text().splitlines()
+    pos = 0
+
+    def section(name):
+        nonlocal pos
+        while pos < len(lines) and lines[pos].strip() != name:
+            pos += 1
+        if pos == len(lines):
+            raise MeshFormatError(f"{filename}: no {name} section")
+        pos += 1
+
+    section("$MeshFormat")
+    version, file_type, _ = lines[pos].split()
+    if not version.startswith("2"):
+        raise MeshFormatError(f"{filename}: MSH {version} is not read "
+                              "(MSH 2.x only)")
+    if file_type != "0":
+        raise MeshFormatError(f"{filename}: binary MSH is not read")
+    section("$Nodes")
+    nnodes = int(lines[pos])
+    rows = np.array([ln.split() for ln in lines[pos + 1:pos + 1 + nnodes]],
+                    dtype=np.float64).reshape(nnodes, 4)
+    pos += 1 + nnodes
+    ids = rows[:, 0].astype(np.int64)
+    points = np.ascontiguousarray(rows[:, 1:4])
+    index = np.full(int(ids.max()) + 1 if nnodes else 1, -1, dtype=np.int64)
+    index[ids] = np.arange(nnodes)
+    section("$Elements")
+    nelem = int(lines[pos])
+    groups = {}
+    for ln in lines[pos + 1:pos + 1 + nelem]:
+        v = ln.split()
+        etype, ntags = int(v[1]), int(v[2])
+        if etype not in MSH_ELEMENTS:
+            raise MeshFormatError(f"{filename}: element type {etype}")
+        name, nv = MSH_ELEMENTS[etype]
+        nodes = [int(x) for x in v[3 + ntags:3 + ntags + nv]]
+        groups.setdefault(name, []).append(nodes)
+    cells_dict = {}
+    for name, conn in groups.items():
+        c = index[np.array(conn, dtype=np.int64)]
+        if np.any(c < 0):
+            raise MeshFormatError(f"{filename}: element refers to a "
+                                  "missing node")
+        cells_dict[name] = c
+    return Mesh(points, cells_dict)
+
+
+def read_mesh(filename):
+    """Read a ``.msh`` (Gmsh MSH 2.x) or legacy ``.vtk`` mesh."""
+    if str(filename).lower().endswith(".msh"):
+        return read_msh(filename)
+    return read_vtk(filename)

@@ -5,8 +5,8 @@ and return values as PeriPy's ``peripy/model.py:24-1575``; the time step
 itself runs in the integrator (``integrators.py``).  Host-side differences,
 all outside the time step:
 
-* meshes are read with the legacy-VTK reader of :mod:`.mesh` (meshio is not
-  a dependency; ``.msh`` files are not read);
+* meshes are read with the legacy-VTK and Gmsh MSH 2.x readers of
+  :mod:`.mesh` (meshio is not a dependency);
 * the neighbour search runs on the GPU for CUDA integrators
   (:mod:`.neighbours`: a cell grid, one warp per node) and with
   ``scipy.spatial.cKDTree.query_pairs`` otherwise, instead of
@@ -24,7 +24,7 @@ import warnings
 import numpy as np
 
 from .integrators import Integrator
-from .mesh import read_vtk, write_vtk
+from .mesh import read_mesh, write_vtk
 
 _MeshElements = namedtuple("MeshElements", ["connectivity", "boundary"])
 _mesh_elements_2d = _MeshElements(connectivity="triangle", boundary="line")
@@ -314,7 +314,7 @@ class Model(object):
     # ------------------------------------------------------------------ mesh
     def _read_mesh(self, filename, transfinite):
         """Read nodes and cells (``peripy/model.py:481-503``)."""
-        mesh = read_vtk(filename)
+        mesh = read_mesh(filename)
         self.coords = np.array(mesh.points, dtype=np.float64)
         self.nnodes = self.coords.shape[0]
         if not transfinite:
