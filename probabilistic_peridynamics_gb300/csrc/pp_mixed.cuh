@@ -442,6 +442,198 @@ __device__ __forceinline__ void bond_phase_node(const pp_fused_args& a, const Mi
     if ((lane & 7) == 0) reinterpret_cast<float*>(&sh.frc[li])[lane >> 3] = v;
 }
 
+// Sum (x, y, z, w) over each group of 8 lanes (lanes 8g .. 8g + 7): 4
+// shuffles.  Lanes 8g + 2c and 8g + 2c + 1 end with channel c (x, y, z, w).
+__device__ __forceinline__ float reduce4_8(float x, float y, float z, float w, int lane) {
+    const bool b2 = lane & 4;
+    const float a_keep = b2 ? z : x, a_send = b2 ? x : z;
+    const float b_keep = b2 ? w : y, b_send = b2 ? y : w;
+    const float p = a_keep + __shfl_xor_sync(kFull, a_send, 4);
+    const float q = b_keep + __shfl_xor_sync(kFull, b_send, 4);
+    const bool b1 = lane & 2;
+    float v = (b1 ? q : p) + __shfl_xor_sync(kFull, b1 ? p : q, 2);
+    v += __shfl_xor_sync(kFull, v, 1);
+    return v;
+}
+
+// reduce4_8 on compensated pairs, rounded once at the end.
+__device__ __forceinline__ float reduce4c_8(float x, float cx, float y, float cy, float z,
+                                            float cz, float w, int lane) {
+    const bool b2 = lane & 4;
+    float p = b2 ? z : x, pc = b2 ? cz : cx;
+    float q = b2 ? w : y, qc = b2 ? 0.f : cy;
+    const float ps = b2 ? x : z, psc = b2 ? cx : cz;
+    const float qs = b2 ? y : w, qsc = b2 ? cy : 0.f;
+    two_sum_into(p, pc, __shfl_xor_sync(kFull, ps, 4), __shfl_xor_sync(kFull, psc, 4));
+    two_sum_into(q, qc, __shfl_xor_sync(kFull, qs, 4), __shfl_xor_sync(kFull, qsc, 4));
+    const bool b1 = lane & 2;
+    float v = b1 ? q : p, vc = b1 ? qc : pc;
+    two_sum_into(v, vc, __shfl_xor_sync(kFull, b1 ? p : q, 2),
+                 __shfl_xor_sync(kFull, b1 ? pc : qc, 2));
+    two_sum_into(v, vc, __shfl_xor_sync(kFull, v, 1), __shfl_xor_sync(kFull, vc, 1));
+    return __fadd_rn(v, vc);
+}
+
+// Bond phase of four nodes per warp, eight lanes each (rows of 64 or more
+// slots).  The group of lanes 8g .. 8g + 7 works on node i (local li) and
+// lane 8g + t takes slots t, t + 8, ..., SPL of them, G at a time.  The
+// warp's four nodes are consecutive, so one gather instruction reaches the
+// first neighbours of four neighbouring nodes: mostly the same L1 lines.
+// i >= nnodes: no node; the lanes only join the warp's shuffles.
+template <int SPL, int G, bool CORR, bool TYPES, bool COMP, class Shared>
+__device__ __forceinline__ void bond_phase_group(const pp_fused_args& a, const MixedConst& c,
+                                                 const Thresholds& th0, Shared& sh, int parity,
+                                                 int i, int li, int lane) {
+    constexpr int LPN = 8;
+    const int sub = lane & (LPN - 1);
+    const bool node_ok = i < a.nnodes;
+    const int ie = node_ok ? i : 0;
+    const int L = a.max_neigh;
+    const int nr = a.nregimes;
+    const float* __restrict__ rec = a.rec[parity];
+    const Rec ri = load_rec(rec, ie);
+    const int4 qi = ri.q;
+    const float4 ui = ri.u;
+    // critical stretch of this node (per instance when batched)
+    float s0f = c.s0, s0err = c.s0_err;
+    double s0d = a.critical_stretch;
+    Thresholds th = th0;
+    if (!TYPES && a.node_instance) {
+        const int inst = a.node_instance[ie];
+        s0f = sh.thr[inst];
+        s0err = 6.0e-8f * fabsf(s0f);
+        s0d = a.instance_s0[inst];
+        th.lo = sh.tlo[inst];
+        th.hi = sh.thi[inst];
+    }
+    const int64_t g0 = (int64_t)ie * L + sub;
+    int32_t* const nl_g = a.nlist + g0;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    float cx = 0.f, cy = 0.f, cz = 0.f;  // carries (COMP)
+    float cnt = 0.f;
+    unsigned amb = 0u;
+#pragma unroll
+    for (int k0 = 0; k0 < SPL; k0 += G) {
+        int jr[G];
+        float sc[G];
+        int bt[G], rg[G];
+#pragma unroll
+        for (int kk = 0; kk < G; ++kk) {
+            const int k = k0 + kk;
+            jr[kk] = node_ok ? load_slot(nl_g + LPN * k) : -1;
+            if constexpr (CORR) sc[kk] = node_ok ? __ldcs(a.sc32 + g0 + LPN * k) : 0.f;
+            if constexpr (TYPES) {
+                bt[kk] = jr[kk] != -1 ? __ldcs(a.bond_types + g0 + LPN * k) * nr : 0;
+                rg[kk] = jr[kk] != -1 ? a.regimes[g0 + LPN * k] : 0;
+            }
+        }
+        int4 qj[G];
+        float4 uj[G];
+#pragma unroll
+        for (int kk = 0; kk < G; ++kk) {
+            const Rec rj = load_rec(rec, jr[kk] < 0 ? ie : jr[kk]);
+            qj[kk] = rj.q;
+            uj[kk] = rj.u;
+        }
+#pragma unroll
+        for (int kk = 0; kk < G; ++kk) {
+            const int k = k0 + kk;
+            const bool valid = jr[kk] != -1;
+            const Bond32 b = bond32(qi, ui, qj[kk], uj[kk], c);
+            float w = __int_as_float(qj[kk].w);  // k*vol (PMB) or vol (types)
+            bool intact;
+            if constexpr (!TYPES) {
+                // clearly intact below th.lo; every other bond is decided in
+                // the slow path below, where breaks are written
+                intact = valid && b.s < th.lo;
+                if (valid && !intact) amb |= 1u << k;
+                w *= b.s;
+            } else {
+                if (!valid) continue;
+                bool ambiguous = false;
+                const int reg = next_regime(rg[kk], bt[kk], nr, [&](int idx) {
+                    if (b.s < sh.tlo[idx]) return true;
+                    if (b.s > sh.thi[idx]) return false;
+                    const float thr = sh.thr[idx];
+                    const float d = b.s - thr;
+                    if (!(fabsf(d) > band32(ui, uj[kk], b, c) + 6.0e-8f * fabsf(thr)))
+                        ambiguous = true;
+                    return d < 0.0f;
+                });
+                if (ambiguous) {
+                    amb |= 1u << k;
+                    continue;
+                }
+                if (reg != rg[kk]) a.regimes[g0 + LPN * k] = reg;
+                intact = reg < nr;
+                if (!intact) {
+                    nl_g[LPN * k] = -1;
+                    continue;
+                }
+                w *= fmaf(b.s, sh.k[bt[kk] + reg], sh.c[bt[kk] + reg]);
+            }
+            float fv = intact ? w * b.ry : 0.0f;
+            if constexpr (CORR) fv *= sc[kk];
+            acc_mul<COMP>(sx, cx, fv, b.px);
+            acc_mul<COMP>(sy, cy, fv, b.py);
+            acc_mul<COMP>(sz, cz, fv, b.pz);
+            cnt += intact ? 1.0f : 0.0f;
+        }
+    }
+    // Slow path: slots that break, or whose FP32 stretch is too close to a
+    // critical stretch.  Their indices, records and tables are read again
+    // (the hot loop keeps nothing for them; no slot was written yet).
+    if (__any_sync(kFull, amb != 0u)) {
+#pragma unroll 1
+        for (int k = 0; k < SPL; ++k) {
+            if (!((amb >> k) & 1u)) continue;
+            const int j = load_slot(nl_g + LPN * k);
+            const Rec rj = load_rec(rec, j);
+            const Bond32 b = bond32(qi, ui, rj.q, rj.u, c);
+            float w = __int_as_float(rj.q.w);
+            bool intact;
+            if constexpr (!TYPES) {
+                // clearly broken, or the bond's own error band decides;
+                // else binary64
+                const float d = b.s - s0f;
+                if (b.s > th.hi)
+                    intact = false;
+                else if (fabsf(d) > band32(ui, rj.u, b, c) + s0err)
+                    intact = d < 0.0f;
+                else
+                    intact = exact_stretch(a, parity, i, j) < s0d;
+                w *= b.s;
+            } else {
+                const double s64 = exact_stretch(a, parity, i, j);
+                const int btk = __ldcs(a.bond_types + g0 + LPN * k) * nr;
+                const int rgk = a.regimes[g0 + LPN * k];
+                const int reg = next_regime(rgk, btk, nr, [&](int idx) {
+                    return s64 < a.critical_stretch_table[idx];
+                });
+                if (reg != rgk) a.regimes[g0 + LPN * k] = reg;
+                intact = reg < nr;
+                if (intact) w *= fmaf(b.s, sh.k[btk + reg], sh.c[btk + reg]);
+            }
+            if (!intact) {
+                nl_g[LPN * k] = -1;
+                continue;
+            }
+            float fv = w * b.ry;
+            if constexpr (CORR) fv *= __ldcs(a.sc32 + g0 + LPN * k);
+            acc_mul<COMP>(sx, cx, fv, b.px);
+            acc_mul<COMP>(sy, cy, fv, b.py);
+            acc_mul<COMP>(sz, cz, fv, b.pz);
+            cnt += 1.0f;
+        }
+    }
+    float v;
+    if constexpr (COMP)
+        v = reduce4c_8(sx, cx, sy, cy, sz, cz, cnt, lane);
+    else
+        v = reduce4_8(sx, sy, sz, cnt, lane);
+    if (node_ok && (sub & 1) == 0) reinterpret_cast<float*>(&sh.frc[li])[sub >> 1] = v;
+}
+
 // Node phase of one chunk: thread (node, component) updates one DOF.
 template <class Shared>
 __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedConst& c,
@@ -560,6 +752,24 @@ __global__ void __launch_bounds__(W * 32, MINB)
     __syncthreads();
     const StepMags m = step_mags(l);
     const Thresholds th0 = thresholds(c.s0, c.s0_err, qb);
+    if constexpr (SL >= 2) {
+        // four consecutive nodes per warp, eight lanes each
+        for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+            const int node0 = chunk * kChunk;
+            for (int t = 0; t < kNodesPerWarp / 4; ++t) {
+                const int first = (t * W + warp) * 4;
+                if (node0 + first >= a.nnodes) break;  // warp-uniform
+                const int li = first + (lane >> 3);
+                bond_phase_group<SL * 4, 4, CORR, TYPES, COMP>(a, c, th0, sh, parity, node0 + li,
+                                                               li, lane);
+            }
+            __syncthreads();
+            for (int li = threadIdx.x >> 2; li < kChunk; li += blockDim.x >> 2)
+                node_phase(a, c, sh, m, parity, node0, li);
+            __syncthreads();
+        }
+        return;
+    }
     const bool has = SL > 1 || lane < L;
     // neighbour slots of node i (-1 beyond the row or past the last node)
     auto load_row = [&](int i, int (&jr)[SL]) {
