@@ -46,6 +46,7 @@ namespace mixed {
 
 constexpr int kMaxTable = 256;
 constexpr int kNodesPerWarp = 16;  // a CTA of W warps owns chunks of 16*W nodes
+constexpr int kLanesPerNode = 8;   // rows of 64+ slots: 32/8 nodes per warp
 
 constexpr int kMagicI = 0x4B400000;  // bit pattern of 1.5 * 2^23
 constexpr float kMagicF = 12582912.0f;
@@ -474,17 +475,46 @@ __device__ __forceinline__ float reduce4c_8(float x, float cx, float y, float cy
     return __fadd_rn(v, vc);
 }
 
+// Sum (x, y, z, w) over each group of LPN lanes (8 or 16): channel c ends
+// in lanes 2c and 2c + 1 of the group (reduce4_8 after one more stage).
+template <int LPN>
+__device__ __forceinline__ float reduce4_group(float x, float y, float z, float w, int lane) {
+    if constexpr (LPN == 16) {
+        x += __shfl_xor_sync(kFull, x, 8);
+        y += __shfl_xor_sync(kFull, y, 8);
+        z += __shfl_xor_sync(kFull, z, 8);
+        w += __shfl_xor_sync(kFull, w, 8);
+    }
+    return reduce4_8(x, y, z, w, lane);
+}
+
+template <int LPN>
+__device__ __forceinline__ float reduce4c_group(float x, float cx, float y, float cy, float z,
+                                                float cz, float w, int lane) {
+    if constexpr (LPN == 16) {
+        two_sum_into(x, cx, __shfl_xor_sync(kFull, x, 8), __shfl_xor_sync(kFull, cx, 8));
+        two_sum_into(y, cy, __shfl_xor_sync(kFull, y, 8), __shfl_xor_sync(kFull, cy, 8));
+        two_sum_into(z, cz, __shfl_xor_sync(kFull, z, 8), __shfl_xor_sync(kFull, cz, 8));
+        w += __shfl_xor_sync(kFull, w, 8);
+    }
+    return reduce4c_8(x, cx, y, cy, z, cz, w, lane);
+}
+
 // Bond phase of four nodes per warp, eight lanes each (rows of 64 or more
 // slots).  The group of lanes 8g .. 8g + 7 works on node i (local li) and
 // lane 8g + t takes slots t, t + 8, ..., SPL of them, G at a time.  The
 // warp's four nodes are consecutive, so one gather instruction reaches the
 // first neighbours of four neighbouring nodes: mostly the same L1 lines.
 // i >= nnodes: no node; the lanes only join the warp's shuffles.
-template <int SPL, int G, bool CORR, bool TYPES, bool COMP, class Shared>
+//
+// jn holds the first G slot indices of this lane (loaded ahead); each batch
+// loads the next batch's indices before its own arithmetic, and the last
+// one loads the first batch of node i_next.
+template <int LPN, int SPL, int G, bool CORR, bool TYPES, bool COMP, class Shared>
 __device__ __forceinline__ void bond_phase_group(const pp_fused_args& a, const MixedConst& c,
                                                  const Thresholds& th0, Shared& sh, int parity,
-                                                 int i, int li, int lane) {
-    constexpr int LPN = 8;
+                                                 int i, int li, int lane, int (&jn)[G],
+                                                 int i_next) {
     const int sub = lane & (LPN - 1);
     const bool node_ok = i < a.nnodes;
     const int ie = node_ok ? i : 0;
@@ -518,9 +548,20 @@ __device__ __forceinline__ void bond_phase_group(const pp_fused_args& a, const M
         float sc[G];
         int bt[G], rg[G];
 #pragma unroll
+        for (int kk = 0; kk < G; ++kk) jr[kk] = jn[kk];
+        if (k0 + G < SPL) {
+#pragma unroll
+            for (int kk = 0; kk < G; ++kk)
+                jn[kk] = node_ok ? load_slot(nl_g + LPN * (k0 + G + kk)) : -1;
+        } else {
+            const int64_t gn = (int64_t)i_next * L + sub;
+#pragma unroll
+            for (int kk = 0; kk < G; ++kk)
+                jn[kk] = i_next < a.nnodes ? load_slot(a.nlist + gn + LPN * kk) : -1;
+        }
+#pragma unroll
         for (int kk = 0; kk < G; ++kk) {
             const int k = k0 + kk;
-            jr[kk] = node_ok ? load_slot(nl_g + LPN * k) : -1;
             if constexpr (CORR) sc[kk] = node_ok ? __ldcs(a.sc32 + g0 + LPN * k) : 0.f;
             if constexpr (TYPES) {
                 bt[kk] = jr[kk] != -1 ? __ldcs(a.bond_types + g0 + LPN * k) * nr : 0;
@@ -628,10 +669,11 @@ __device__ __forceinline__ void bond_phase_group(const pp_fused_args& a, const M
     }
     float v;
     if constexpr (COMP)
-        v = reduce4c_8(sx, cx, sy, cy, sz, cz, cnt, lane);
+        v = reduce4c_group<LPN>(sx, cx, sy, cy, sz, cz, cnt, lane);
     else
-        v = reduce4_8(sx, sy, sz, cnt, lane);
-    if (node_ok && (sub & 1) == 0) reinterpret_cast<float*>(&sh.frc[li])[sub >> 1] = v;
+        v = reduce4_group<LPN>(sx, sy, sz, cnt, lane);
+    if (node_ok && sub < 8 && (sub & 1) == 0)
+        reinterpret_cast<float*>(&sh.frc[li])[sub >> 1] = v;
 }
 
 // Node phase of one chunk: thread (node, component) updates one DOF.
@@ -753,15 +795,29 @@ __global__ void __launch_bounds__(W * 32, MINB)
     const StepMags m = step_mags(l);
     const Thresholds th0 = thresholds(c.s0, c.s0_err, qb);
     if constexpr (SL >= 2) {
-        // four consecutive nodes per warp, eight lanes each
+        // kNPW consecutive nodes per warp, kLPN lanes each
+        constexpr int kLPN = kLanesPerNode;
+        constexpr int kNPW = 32 / kLPN;
+        constexpr int kG = 4;
+        const int grp = lane / kLPN, sub = lane % kLPN;
+        auto first_batch = [&](int i, int (&jn)[kG]) {
+#pragma unroll
+            for (int kk = 0; kk < kG; ++kk)
+                jn[kk] = i < a.nnodes ? load_slot(a.nlist + (int64_t)i * L + sub + kLPN * kk) : -1;
+        };
+        int jn[kG];
+        first_batch(blockIdx.x * kChunk + warp * kNPW + grp, jn);
         for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
             const int node0 = chunk * kChunk;
-            for (int t = 0; t < kNodesPerWarp / 4; ++t) {
-                const int first = (t * W + warp) * 4;
+            for (int t = 0; t < kNodesPerWarp / kNPW; ++t) {
+                const int first = (t * W + warp) * kNPW;
                 if (node0 + first >= a.nnodes) break;  // warp-uniform
-                const int li = first + (lane >> 3);
-                bond_phase_group<SL * 4, 4, CORR, TYPES, COMP>(a, c, th0, sh, parity, node0 + li,
-                                                               li, lane);
+                const int li = first + grp;
+                const int i_next = t + 1 < kNodesPerWarp / kNPW
+                                       ? node0 + li + W * kNPW
+                                       : (chunk + gridDim.x) * kChunk + warp * kNPW + grp;
+                bond_phase_group<kLPN, SL * 32 / kLPN, kG, CORR, TYPES, COMP>(
+                    a, c, th0, sh, parity, node0 + li, li, lane, jn, i_next);
             }
             __syncthreads();
             for (int li = threadIdx.x >> 2; li < kChunk; li += blockDim.x >> 2)
