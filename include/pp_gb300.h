@@ -192,10 +192,10 @@ typedef struct pp_fused_args {
     int32_t flags;                 /* PP_FLAG_* bits; others must be 0     */
     int32_t nodes_per_block;       /* PP_FLOAT64: warps per block (0 = 8)  */
     int32_t variant;               /* PP_MIXED tile shape, 0..PP_MIXED_VARIANTS-1:
-                                      0: 8 warps x 128 nodes per CTA,
-                                      register budget for 3 resident CTAs
+                                      0: 4 warps x 64 nodes per CTA,
+                                      register budget for 8 resident CTAs
                                       per SM; 1: 8 warps x 128 nodes, 4
-                                      CTAs/SM; 2: 4 warps x 64 nodes, 6
+                                      CTAs/SM; 2: 8 warps x 128 nodes, 3
                                       CTAs/SM                             */
     int32_t reserved;              /* must be 0                            */
     double dt;
