@@ -5,21 +5,24 @@
 // load per bond, the break / regime decision taken exactly as binary64
 // would on the same state, and double-float node state.
 //
-// Structure of one launch (one CTA = W warps, chunks of 8 W consecutive
+// Structure of one launch (one CTA = W warps, chunks of 16 W consecutive
 // nodes, persistent over the chunks):
 //
-//  1. Bond phase, one warp per node (the CTA's warps working on W
-//     consecutive nodes at a time so their neighbourhoods share L1 lines;
-//     no shared-memory staging, so L1 keeps its full capacity for the
-//     records).  Lane l takes slots l, l + 32, ...: the neighbour indices
-//     were loaded while the warp worked on its previous node; then all
-//     record gathers, then the FP32 bond arithmetic.  A slot whose FP32
-//     stretch lies within the proven error band of a critical stretch is
-//     deferred to a slow path that evaluates the binary64 stretch of
-//     peridynamics.cl:65-75 from the reference r0 and the exact
-//     double-float displacement.  The four per-node sums (force x, y, z and
-//     the intact count) are reduced with a 6-shuffle transposed butterfly
-//     and parked in shared memory.
+//  1. Bond phase.  Rows of 64 or more slots: four consecutive nodes per
+//     warp, eight lanes per node, lane t taking slots t, t + 8, ... four at
+//     a time (bond_phase_group); the slot indices of the next batch are
+//     loaded while a batch computes, and one gather instruction reaches the
+//     first neighbours of four neighbouring nodes, mostly the same L1
+//     lines.  Rows of 32 slots or fewer: one warp per node, lane l taking
+//     slot l (bond_phase_node).  Each slot costs one 256-bit record gather
+//     and the FP32 bond arithmetic; a clearly intact bond is decided by one
+//     compare, every other one (breaking, or close to a critical stretch)
+//     in a per-node slow path, where the bond's own error band or else the
+//     binary64 stretch of peridynamics.cl:65-75, from the reference r0 and
+//     the exact double-float displacement, decides.  The four per-node sums
+//     (force x, y, z and the intact count) are reduced with a transposed
+//     butterfly and parked in shared memory.  No shared-memory staging of
+//     the neighbour list, so L1 keeps its full capacity for the records.
 //  2. Node phase, all threads: thread (node, component) applies the force
 //     boundary condition and the integrator update of one DOF in
 //     double-float arithmetic and writes one word of each half of the
