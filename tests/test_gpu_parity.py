@@ -375,3 +375,38 @@ def test_fused_run_graph_matches_steps():
                                        use_run=use_run))
         for a, b in zip(*outs):
             assert np.array_equal(a, b)
+
+
+# ------------------------------------------------------ every row width
+@pytest.mark.parametrize("factor,width", [(1.0, 8), (2.0, 32), (2.3, 64),
+                                          (3.015, 128), (3.5, 256)])
+@pytest.mark.parametrize("mode", ["fused64", "mixed"])
+def test_row_widths(factor, width, mode):
+    """Rows of 8 to 256 slots: both bond-phase layouts of the mixed kernel
+    (one warp per node up to 32 slots, four nodes per warp beyond) and the
+    FP64 kernel's slot loops, with load-induced breaking."""
+    import probabilistic_peridynamics_gb300 as pp
+    coords, volume, horizon, family, nlist, n_neigh = lattice(9, 8, 8, 1.0,
+                                                              factor)
+    assert nlist.shape[1] == width
+    bc_types, bc_values = pull_bcs(coords, 0)
+    n = coords.shape[0]
+    setup = dict(coords=coords, volume=volume, family=family, nlist=nlist,
+                 n_neigh=n_neigh, bc_types=bc_types, bc_values=bc_values,
+                 force_bc_types=np.zeros((n, 3), dtype=np.intc),
+                 force_bc_values=np.zeros((n, 3)), nnodes=n, max_neigh=width,
+                 k=0.01 * 122.0 / max(int(family.max()), 1), s0=0.02, dt=0.5)
+    steps = 40
+    mags = 4e-3 * np.arange(1, steps + 1)
+    integ = pp.EulerCUDA(dt=setup["dt"], fused=True,
+                         precision="mixed" if mode == "mixed" else "float64")
+    out = run_integrator(integ, setup, steps, mags)
+    ref = run_oracle("euler", setup, steps, mags)
+    assert int((nlist != -1).sum() - (ref[6] != -1).sum()) > 0
+    if mode == "mixed":
+        assert int((out[6] != ref[6]).sum()) == 0
+        assert np.array_equal(out[7], ref[7])
+        assert rel_err(out[0], ref[0]) < MIXED_TOL
+    else:
+        for got, want in zip(out, ref):
+            assert np.array_equal(got, want)
