@@ -446,6 +446,23 @@ def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None, ny=NY):
     return bonds * done / el, done, el, bonds, kind, cores, bonds - intact()
 
 
+def host_cpu():
+    """Model name and core count of the host, for the CPU lines."""
+    model = None
+    try:
+        for line in pathlib.Path("/proc/cpuinfo").read_text().splitlines():
+            key = line.split(":")[0].strip().lower()
+            if key in ("model name", "cpu model", "hardware") and ":" in line:
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    if not model:
+        import platform
+        model = platform.processor() or platform.machine()
+    return {"cpu": model, "host_cores": os.cpu_count()}
+
+
 def cpu_baseline():
     rate, steps, el, bonds, kind, cores, broken = cpu_sample(NX,
                                                              budget_s=10.0)
@@ -453,6 +470,7 @@ def cpu_baseline():
             " + bond_force + update_displacement)" if kind == "reference"
             else "C restatement of the OpenCL step (OpenMP)")
     return {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
+            **host_cpu(),
             "sample": f"{steps} step(s) of the {what} on the full "
                       f"{NX}x{NY}x{NZ} lattice ({bonds} bonds/step, Euler "
                       f"dt {CPU_DT:g}, {broken} bonds broken), {el:.1f} s"}
@@ -492,7 +510,7 @@ def reference_arm(args):
                    "integrator": "Euler (the reference CPU path has no "
                                  "Velocity-Verlet)"},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores,
-                         "kind": kind, "sample": sample},
+                         "kind": kind, **host_cpu(), "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
