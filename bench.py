@@ -25,8 +25,9 @@ Arms
 ``python bench.py --impl reference ...``
     The reference's own CPU step (``peripy/peridynamics.pyx`` break_bonds +
     bond_force + update_displacement, as ``Euler.__call__`` calls them),
-    compiled from its sources into ``oracle/_ref``, on a bounded slab of the
-    same lattice per step.
+    compiled from its sources into ``oracle/_ref``, on a bounded block
+    (4 x ny x 10) of the same lattice per step, pulled at the plate's strain
+    rate, with a stable Euler pseudo-step (see ``CPU_DT``).
 
 Under torchrun every rank runs an independent replica on its own GPU (the
 configuration fits one GPU); ``value`` is the sum over ranks.
@@ -86,7 +87,8 @@ def parse_args():
                    default="large",
                    help="large: the 200x200x10 Velocity-Verlet plate (the "
                         "headline); batched: 64 uneven UQ instances, "
-                        "Euler-Cromer")
+                        "Euler-Cromer; composite: 1M Poisson-disk points, "
+                        "three bond types, trilinear damage")
     p.add_argument("--profile", choices=["mixed", "fp64", "plain"],
                    help="only run 3 warm-up and 3 profiled launches of one "
                         "step variant on the full workload (for ncu)")
