@@ -410,3 +410,47 @@ def test_row_widths(factor, width, mode):
     else:
         for got, want in zip(out, ref):
             assert np.array_equal(got, want)
+
+
+# ------------------------------------------------- force boundary conditions
+@pytest.mark.parametrize("kind", list(_KINDS))
+@pytest.mark.parametrize("mode", ["plain", "fused64", "mixed", "mixed_run"])
+def test_force_boundary_conditions(kind, mode):
+    """A force on the x-max face (F / vol / n_face per node, as
+    ``_set_boundary_conditions`` spreads it, ``peripy/model.py:1194-1209``)
+    ramped over the steps, the x-min face clamped; bonds break under it."""
+    import probabilistic_peridynamics_gb300 as pp
+    setup = _breaking_setup(kind)
+    coords, vol = setup["coords"], setup["volume"]
+    n = coords.shape[0]
+    right = coords[:, 0] >= coords[:, 0].max() - 1e-9
+    left = coords[:, 0] <= coords[:, 0].min() + 1e-9
+    bc_types = np.zeros((n, 3), dtype=np.intc)
+    bc_types[left] = 1
+    setup["bc_types"], setup["bc_values"] = bc_types, np.zeros((n, 3))
+    fct = np.zeros((n, 3), dtype=np.intc)
+    fcv = np.zeros((n, 3))
+    fct[right, 0] = 1
+    fcv[right, 0] = 1.0 / vol[right] / right.sum()
+    setup["force_bc_types"], setup["force_bc_values"] = fct, fcv
+    steps = 60
+    dmags = np.zeros(steps)
+    fmags = 0.02 * np.arange(1, steps + 1)
+    cls = getattr(pp, _KINDS[kind])
+    kw = dict(fused=mode != "plain",
+              precision="mixed" if mode.startswith("mixed") else "float64")
+    integ = (cls(dt=setup["dt"], **kw) if kind == "euler"
+             else cls(damping=0.5, dt=setup["dt"], **kw))
+    out = run_integrator(integ, setup, steps, dmags, force_mags=fmags,
+                         use_run=mode.endswith("_run"))
+    ref = run_oracle(kind, setup, steps, dmags, force_mags=fmags,
+                     damping=0.0 if kind == "euler" else 0.5)
+    assert int((setup["nlist"] != -1).sum() - (ref[6] != -1).sum()) > 0
+    assert np.any(ref[4][right, 0] != 0.0)  # the force reached the face
+    if mode.startswith("mixed"):
+        assert int((out[6] != ref[6]).sum()) == 0
+        assert rel_err(out[0], ref[0]) < MIXED_TOL
+        assert rel_err(out[4], ref[4]) < MIXED_TOL
+    else:
+        for got, want in zip(out, ref):
+            assert np.array_equal(got, want)
