@@ -454,3 +454,36 @@ def test_force_boundary_conditions(kind, mode):
     else:
         for got, want in zip(out, ref):
             assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("kind", ["euler", "euler_cromer", "velocity_verlet"])
+@pytest.mark.parametrize("mode", ["plain", "fused64", "mixed"])
+def test_nonuniform_volumes_and_densities(kind, mode):
+    """Node volumes (bond weights k*vol_j) and densities that differ per
+    node and per component, with breaking."""
+    import probabilistic_peridynamics_gb300 as pp
+    setup = _breaking_setup(kind)
+    n = setup["nnodes"]
+    rng = np.random.default_rng(11)
+    setup["volume"] = rng.uniform(0.7, 1.3, n)
+    if kind != "euler":
+        setup["densities"] = rng.uniform(30.0, 70.0, (n, 3))
+    steps = 60
+    mags = 3e-3 * np.arange(1, steps + 1)
+    cls = getattr(pp, _KINDS[kind])
+    kw = dict(fused=mode != "plain",
+              precision="mixed" if mode == "mixed" else "float64")
+    integ = (cls(dt=setup["dt"], **kw) if kind == "euler"
+             else cls(damping=0.5, dt=setup["dt"], **kw))
+    out = run_integrator(integ, setup, steps, mags)
+    ref = run_oracle(kind, setup, steps, mags,
+                     damping=0.0 if kind == "euler" else 0.5)
+    assert int((setup["nlist"] != -1).sum() - (ref[6] != -1).sum()) > 0
+    if mode == "mixed":
+        assert int((out[6] != ref[6]).sum()) == 0
+        assert rel_err(out[0], ref[0]) < MIXED_TOL
+        if kind != "euler":
+            assert rel_err(out[1], ref[1]) < MIXED_TOL
+    else:
+        for got, want in zip(out, ref):
+            assert np.array_equal(got, want)
