@@ -83,12 +83,14 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--accuracy-steps", type=int, default=E2E_STEPS)
-    p.add_argument("--workload", choices=["large", "batched", "composite"],
+    p.add_argument("--workload",
+                   choices=["large", "batched", "composite", "adjoint"],
                    default="large",
                    help="large: the 200x200x10 Velocity-Verlet plate (the "
                         "headline); batched: 64 uneven UQ instances, "
                         "Euler-Cromer; composite: 1M Poisson-disk points, "
-                        "three bond types, trilinear damage")
+                        "three bond types, trilinear damage; adjoint: "
+                        "forward + backward passes of the 50x50x5 rollout")
     p.add_argument("--profile", choices=["mixed", "fp64", "plain"],
                    help="only run 3 warm-up and 3 profiled launches of one "
                         "step variant on the full workload (for ncu)")
@@ -707,6 +709,63 @@ def composite_main(args):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_main(args):
+    """Gradient of a displacement loss through the Euler rollout: the
+    50x50x5 lattice (dx 1, horizon 3.015, per-bond stiffness 0.01 U(0.9,1.1)
+    as a float32 parameter), faces pulled 1e-9 per step, dt 0.5, 500 steps,
+    checkpoint every 50, loss = sum of squared displacements of 100 seeded
+    probe nodes.  One step of this line = one forward + backward pass."""
+    import torch
+    from probabilistic_peridynamics_gb300 import lattice
+    from probabilistic_peridynamics_gb300.adjoint import (AdjointProblem,
+                                                          rollout)
+    nx, ny, nz, steps, every = 50, 50, 5, 500, 50
+    coords = lattice.lattice_coords(nx, ny, nz, 1.0)
+    family, nlist, _ = lattice.lattice_family(nx, ny, nz, HORIZON_CELLS)
+    bc_types, bc_values = lattice.face_bcs(coords, 0)
+    n = coords.shape[0]
+    prob = AdjointProblem(coords, np.ones(n), nlist, bc_types, bc_values,
+                          1e-9 * np.arange(1, steps + 1), 0.5)
+    rng = np.random.default_rng(4)
+    probes = torch.tensor(rng.choice(n, 100, replace=False), device="cuda")
+    k0 = np.where(nlist != -1, 0.01 * rng.uniform(0.9, 1.1, nlist.shape),
+                  0.0)
+    k = torch.tensor(k0, dtype=torch.float32, device="cuda",
+                     requires_grad=True)
+
+    def one():
+        k.grad = None
+        u = rollout(k, 1.0, prob, steps, every)
+        (u[probes] ** 2).sum().backward()
+
+    for _ in range(args.warmup):
+        one()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        one()
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    bonds = int(family.sum())
+    # forward steps + recomputed forward steps + reverse steps per pass
+    updates = bonds * steps * 3
+    line = {
+        "metric": "adjoint passes/s (forward + checkpointed backward)",
+        "value": 1e3 / ms, "unit": "passes/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "adjoint: 50x50x5 lattice, 500 Euler steps, "
+                               "checkpoint every 50, 100 probes",
+                   "nodes": n, "bonds": bonds,
+                   "bond_updates_per_s": updates / (ms * 1e-3)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.profile:
@@ -720,6 +779,9 @@ def main():
         return
     if args.workload == "composite":
         composite_main(args)
+        return
+    if args.workload == "adjoint":
+        adjoint_main(args)
         return
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
