@@ -190,7 +190,7 @@ typedef struct pp_fused_args {
     int32_t nregimes;
     int32_t nbond_types;
     int32_t flags;                 /* PP_FLAG_* bits; others must be 0     */
-    int32_t nodes_per_block;       /* PP_FLOAT64: warps per block (0 = 8)  */
+    int32_t nodes_per_block;       /* PP_FLOAT64: warps per block, 1..8 (0 = 8) */
     int32_t variant;               /* PP_MIXED tile shape, 0..PP_MIXED_VARIANTS-1:
                                       0: 4 warps x 64 nodes per CTA,
                                       register budget for 8 resident CTAs

@@ -21,67 +21,87 @@ namespace {
 
 constexpr int kDefaultWarps = 8;
 
+// One warp per node for the bond phase; the node updates of the block's
+// nodes then run one thread per DOF (the update's binary64 instructions
+// would otherwise occupy GB300's FP64 pipe for a whole warp per 3 lanes).
 template <int SL, bool CORR, bool TYPES>
 __global__ void __launch_bounds__(256) k_fused_f64(pp_fused_args a, int parity, Launch l) {
+    __shared__ double s_f[32][3];
+    __shared__ int s_cnt[32];
     const int lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
-    const int i = blockIdx.x * wpb + (threadIdx.x >> 5);
-    if (i >= a.nnodes) return;  // warp-uniform
+    const int warp = threadIdx.x >> 5;
+    const int node0 = blockIdx.x * wpb;
+    const int i = node0 + warp;
     const StepMags m = step_mags(l);
     const double* __restrict__ u = a.u[parity];
-    const F64Bond b{a.r0,
-                    u,
-                    a.vols,
-                    a.nlist,
-                    a.stiffness_corrections,
-                    a.bond_types,
-                    a.regimes,
-                    a.bond_stiffness_table,
-                    a.critical_stretch_table,
-                    a.plus_cs,
-                    a.bond_stiffness,
-                    a.node_instance ? a.instance_s0[a.node_instance[i]] : a.critical_stretch,
-                    a.nregimes};
-    const int64_t o3 = 3 * (int64_t)i;
-    const d3 ri{a.r0[o3], a.r0[o3 + 1], a.r0[o3 + 2]};
-    const d3 ui{u[o3], u[o3 + 1], u[o3 + 2]};
-    const int64_t row = (int64_t)i * a.max_neigh;
-    int intact = 0;
-    const d3 f = tree_reduce_f64<SL>(lane, a.max_neigh, [&](int k) {
-        return f64_slot<CORR, TYPES>(b, row + k, ri, ui, intact);
-    });
-    const int count = __reduce_add_sync(kFull, intact);
-    const double fx = __shfl_sync(kFull, f.x, 0);
-    const double fy = __shfl_sync(kFull, f.y, 0);
-    const double fz = __shfl_sync(kFull, f.z, 0);
-    if (lane < 3) {
-        const int64_t o = o3 + lane;
-        const double body = lane == 0 ? fx : (lane == 1 ? fy : fz);
-        a.body_force[o] = body;
-        const double frc = force_with_bc(body, a.fc_types[o], a.fc_values[o], m.force);
-        a.force[o] = frc;
-        const int bct = a.bc_types[o];
-        const double bcv = a.bc_values[o];
-        double unew;
-        if (a.integrator == PP_EULER) {
-            unew = euler_u(u[o], frc, bct, bcv, m.disp, a.dt);
-        } else {
-            double v = a.ud[o];
-            double acc = a.udd[o];
-            if (a.integrator == PP_EULER_CROMER)
-                unew = euler_cromer_u(u[o], v, acc, frc, bct, bcv, a.densities[o], m.disp,
-                                      a.damping, a.dt);
-            else
-                unew = velocity_verlet_u(u[o], v, acc, frc, bct, bcv, a.densities[o], m.disp,
-                                         a.damping, a.dt);
-            a.ud[o] = v;
-            a.udd[o] = acc;
+    if (i < a.nnodes) {  // warp-uniform
+        const F64Bond b{a.r0,
+                        u,
+                        a.vols,
+                        a.nlist,
+                        a.stiffness_corrections,
+                        a.bond_types,
+                        a.regimes,
+                        a.bond_stiffness_table,
+                        a.critical_stretch_table,
+                        a.plus_cs,
+                        a.bond_stiffness,
+                        a.node_instance ? a.instance_s0[a.node_instance[i]] : a.critical_stretch,
+                        a.nregimes};
+        const int64_t o3 = 3 * (int64_t)i;
+        const d3 ri{a.r0[o3], a.r0[o3 + 1], a.r0[o3 + 2]};
+        const d3 ui{u[o3], u[o3 + 1], u[o3 + 2]};
+        const int64_t row = (int64_t)i * a.max_neigh;
+        int intact = 0;
+        const d3 f = tree_reduce_f64<SL>(lane, a.max_neigh, [&](int k) {
+            return f64_slot<CORR, TYPES>(b, row + k, ri, ui, intact);
+        });
+        const int count = __reduce_add_sync(kFull, intact);
+        if (lane == 0) {
+            s_f[warp][0] = f.x;
+            s_f[warp][1] = f.y;
+            s_f[warp][2] = f.z;
+            s_cnt[warp] = count;
         }
-        a.u[parity ^ 1][o] = unew;
     }
-    if (lane == 0) {
-        a.n_neigh[i] = count;
-        a.damage[i] = damage_of(count, a.family[i]);
+    __syncthreads();
+    const int t = threadIdx.x;
+    if (t < 3 * wpb) {
+        const int li = t / 3, d = t % 3;
+        const int n = node0 + li;
+        if (n < a.nnodes) {
+            const int64_t o = 3 * (int64_t)n + d;
+            const double body = s_f[li][d];
+            a.body_force[o] = body;
+            const double frc = force_with_bc(body, a.fc_types[o], a.fc_values[o], m.force);
+            a.force[o] = frc;
+            const int bct = a.bc_types[o];
+            const double bcv = a.bc_values[o];
+            double unew;
+            if (a.integrator == PP_EULER) {
+                unew = euler_u(u[o], frc, bct, bcv, m.disp, a.dt);
+            } else {
+                double v = a.ud[o];
+                double acc = a.udd[o];
+                if (a.integrator == PP_EULER_CROMER)
+                    unew = euler_cromer_u(u[o], v, acc, frc, bct, bcv, a.densities[o], m.disp,
+                                          a.damping, a.dt);
+                else
+                    unew = velocity_verlet_u(u[o], v, acc, frc, bct, bcv, a.densities[o],
+                                             m.disp, a.damping, a.dt);
+                a.ud[o] = v;
+                a.udd[o] = acc;
+            }
+            a.u[parity ^ 1][o] = unew;
+        }
+    } else if (t < 4 * wpb) {
+        const int n = node0 + (t - 3 * wpb);
+        if (n < a.nnodes) {
+            const int count = s_cnt[t - 3 * wpb];
+            a.n_neigh[n] = count;
+            a.damage[n] = damage_of(count, a.family[n]);
+        }
     }
 }
 
@@ -94,7 +114,7 @@ int validate_fused(const pp_fused_args& a) {
     if (a.nnodes < 0) return PP_ERROR_INVALID_VALUE;
     if (!is_pow2_le_1024(a.max_neigh)) return PP_ERROR_MAX_NEIGH;
     if (a.integrator < PP_EULER || a.integrator > PP_VELOCITY_VERLET) return PP_ERROR_INVALID_VALUE;
-    if (a.nodes_per_block < 0 || a.nodes_per_block > 32) return PP_ERROR_INVALID_VALUE;
+    if (a.nodes_per_block < 0 || a.nodes_per_block > 8) return PP_ERROR_INVALID_VALUE;
     if (a.reserved != 0 || a.reserved2 != 0) return PP_ERROR_INVALID_VALUE;
     if (a.flags & ~PP_FLAG_COMPENSATED) return PP_ERROR_INVALID_VALUE;
     // compensation applies to the FP32 force sums of PP_MIXED only
