@@ -110,7 +110,8 @@ def composite(count=1_000_000, box=(2.0, 1.0, 0.1), spacing=0.004,
               stretches=(0.004, 0.006, 0.01), density=2400.0, seed=5,
               context=None):
     """The irregular composite plate: ``count`` Poisson-disk points in
-    ``box``, horizon ``horizon_factor * spacing``, node volume box/count.
+    ``box``, numbered along a Z-order curve, horizon ``horizon_factor *
+    spacing``, node volume box/count.
 
     Bond types: 0 when both ends lie at x < ``split`` (bulk modulus
     ``bulk_moduli[0]``), 1 when both lie at x >= ``split``
@@ -128,6 +129,10 @@ def composite(count=1_000_000, box=(2.0, 1.0, 0.1), spacing=0.004,
     """
     horizon = horizon_factor * spacing
     coords = poisson_disk((0.0, 0.0, 0.0), box, spacing, count, seed)
+    # number the points along a Z-order curve (random sequential addition
+    # leaves them in random order; a mesher numbers nodes coherently)
+    from .ordering import morton_order
+    coords = coords[morton_order(coords, cell=spacing)]
     n = coords.shape[0]
     if context is not None:
         from .neighbours import neighbour_family
