@@ -314,6 +314,26 @@ int pp_neighbour_rows(const double* coords, int32_t nnodes, double horizon, cons
                       int32_t* family, int32_t* overflow, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Initial crack (set-up).  Replaces peripy/create_crack.pyx:1-43, which    */
+/* Model._set_neighbour_list calls (peripy/model.py:588-595): for each pair  */
+/* (i, j) of crack ((npairs, 2) int32, device) in order, j is removed from  */
+/* row i and then i from row j of nlist ((nnodes, max_neigh) int32, device, */
+/* in/out).  A removal looks for the node among the row's first n_neigh[i]  */
+/* entries; the first match is overwritten by the row's last entry, that    */
+/* slot becomes -1 and n_neigh[i] ((nnodes) int32, device, in/out) drops by */
+/* one; a node that is not found is skipped.  The result is that of the     */
+/* sequential loop.  A negative index selects row nnodes + i, while the     */
+/* node looked for is the other index as given (so a negative one is never */
+/* found), as in the reference.  scratch: nnodes + 1 + 4 * npairs int32 on  */
+/* the device.  An index outside [-nnodes, nnodes) sets *bad (a device      */
+/* word) to 1 and leaves nlist and n_neigh unchanged; else *bad becomes 0.  */
+/* ------------------------------------------------------------------------ */
+
+int pp_create_crack(const int32_t* crack, int32_t npairs, int32_t nnodes, int32_t max_neigh,
+                    int32_t* nlist, int32_t* n_neigh, int32_t* scratch, int32_t* bad,
+                    void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Stiffness correction factors (set-up).  Replaces the correction          */
 /* algorithms of peripy/correction.pyx:5-277 as Model.__init__ applies them */
 /* (peripy/model.py:349-375, 782-935): each selected factor multiplies the  */

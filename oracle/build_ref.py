@@ -4,9 +4,9 @@ INFRASTRUCTURE: the checker and the timed CPU baseline, never the product).
 Recipe
 ------
 1. Where the reference checkout exists (``/root/reference``, read-only),
-   Cython translates ``peripy/peridynamics.pyx``, ``peripy/correction.pyx``
-   and ``peripy/spatial.pyx`` (which the other two cimport through
-   ``spatial.pxd``) from where they lie into C files under
+   Cython translates ``peripy/peridynamics.pyx``, ``peripy/correction.pyx``,
+   ``peripy/create_crack.pyx`` and ``peripy/spatial.pyx`` (which the first
+   two cimport through ``spatial.pxd``) from where they lie into C files under
    ``oracle/_ref/src/``.  Nothing is written
    into the reference tree and no reference source is copied.
 2. gcc compiles each C file with the reference's own flags (``-O3``,
@@ -14,7 +14,8 @@ Recipe
    round one by one as written on every host (aarch64 gcc would otherwise
    fuse multiply-adds that the x86-64 build does not), into
    ``oracle/_ref/peripy/<module>.so``, importable as
-   ``peripy.peridynamics`` / ``peripy.correction`` / ``peripy.spatial`` once
+   ``peripy.peridynamics`` / ``peripy.correction`` /
+   ``peripy.create_crack`` / ``peripy.spatial`` once
    ``oracle/_ref`` is on
    ``sys.path`` (``oracle/_ref/peripy/__init__.py`` is an empty file written
    here so the package imports without the reference's own ``__init__``).
@@ -34,7 +35,7 @@ HERE = pathlib.Path(__file__).resolve().parent
 REF_OUT = HERE / "_ref"
 SRC = REF_OUT / "src"
 PKG = REF_OUT / "peripy"
-MODULES = ("spatial", "peridynamics", "correction")
+MODULES = ("spatial", "peridynamics", "correction", "create_crack")
 DEFAULT_REFERENCE = pathlib.Path("/root/reference")
 
 

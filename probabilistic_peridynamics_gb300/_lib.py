@@ -133,6 +133,8 @@ SIGNATURES = {
                                           _vp]),
     "pp_neighbour_rows": (ctypes.c_int, [_vp, _i32, _f64, _vp, _f64, _vp, _vp,
                                          _vp, _i32, _vp, _vp, _vp, _vp]),
+    "pp_create_crack": (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp, _vp, _vp,
+                                       _vp, _vp]),
     "pp_mixed_pack": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
     "pp_mixed_export": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
     "pp_partner_slots": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp]),

@@ -12,6 +12,8 @@
 // the neighbour indices of a row are distinct).  A pair is a neighbour pair
 // when (dx*dx + dy*dy) + dz*dz <= horizon*horizon in binary64, in that
 // order, with no contraction.
+#include <climits>
+
 #include "pp_common.cuh"
 
 namespace pp {
@@ -152,6 +154,108 @@ __global__ void __launch_bounds__(kRowWarps * 32)
     for (int e = cnt + lane; e < max_neigh; e += 32) out[e] = -1;
 }
 
+// ---- initial crack ---------------------------------------------------------
+// Every pair c = (i, j) of the crack list is two edits: "remove j from row i"
+// with key 2c and "remove i from row j" with key 2c + 1.  The edits are
+// grouped by row with a counting sort (cs: per-row counts, the scan above,
+// a decrement-scatter), and one warp per row applies its edits in key order,
+// which is the order in which the sequential loop over the crack list meets
+// them.  Edits of different rows commute, so the result is the sequential
+// one.
+
+// A pair's index selects a row counting from the end when negative, as an
+// index of the reference's memoryviews does; the node looked for in the
+// other row is the index as given.
+__device__ __forceinline__ int crack_row(int i, int nnodes) { return i < 0 ? i + nnodes : i; }
+
+// cs[row + 1] += 1 for both rows of every pair (cs zeroed by the caller); an
+// index outside [-nnodes, nnodes) sets *bad.
+__global__ void k_crack_count(const int32_t* __restrict__ crack, int npairs, int nnodes,
+                              int32_t* __restrict__ cs, int32_t* bad) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= npairs) return;
+    const int i = crack[2 * (int64_t)c], j = crack[2 * (int64_t)c + 1];
+    if (i < -nnodes || i >= nnodes || j < -nnodes || j >= nnodes) {
+        atomicExch(bad, 1);
+        return;
+    }
+    atomicAdd(&cs[crack_row(i, nnodes) + 1], 1);
+    atomicAdd(&cs[crack_row(j, nnodes) + 1], 1);
+}
+
+// Scatter the edits into their rows' segments (nothing when *bad is set:
+// the crack list is then rejected as a whole).  Afterwards cs[row + 1] is
+// the start of the row's segment.
+__global__ void k_crack_fill(const int32_t* __restrict__ crack, int npairs, int nnodes,
+                             int32_t* __restrict__ cs, const int32_t* __restrict__ bad,
+                             int32_t* __restrict__ key, int32_t* __restrict__ target) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= npairs || *bad) return;
+    const int i = crack[2 * (int64_t)c], j = crack[2 * (int64_t)c + 1];
+    int p = atomicSub(&cs[crack_row(i, nnodes) + 1], 1) - 1;
+    key[p] = 2 * c;
+    target[p] = j;
+    p = atomicSub(&cs[crack_row(j, nnodes) + 1], 1) - 1;
+    key[p] = 2 * c + 1;
+    target[p] = i;
+}
+
+// One warp per row.  Edits are taken in ascending key order (a warp-wide
+// minimum over the keys above the last one applied: keys are distinct).  An
+// edit looks for the target among the row's first n_neigh entries; the
+// first hit takes the row's last entry, whose slot becomes -1, and the count
+// drops by one.  A target that is not found leaves the row as it is.
+__global__ void __launch_bounds__(kRowWarps * 32)
+    k_crack_apply(int nnodes, int max_neigh, int total, const int32_t* __restrict__ cs,
+                  const int32_t* __restrict__ bad, const int32_t* __restrict__ key,
+                  const int32_t* __restrict__ target, int32_t* __restrict__ nlist,
+                  int32_t* __restrict__ n_neigh) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kRowWarps + (threadIdx.x >> 5);
+    if (i >= nnodes || *bad) return;  // warp-uniform
+    const int beg = cs[i + 1];
+    const int end = i + 1 < nnodes ? cs[i + 2] : total;
+    if (beg >= end) return;
+    int32_t* row = nlist + (int64_t)i * max_neigh;
+    int cnt = min(max(n_neigh[i], 0), max_neigh);
+    int last = -1;
+    for (int e = beg; e < end; ++e) {
+        int best = INT_MAX, who = -1;
+        for (int k = beg + lane; k < end; k += 32) {
+            const int v = key[k];
+            if (v > last && v < best) {
+                best = v;
+                who = k;
+            }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            const int ob = __shfl_xor_sync(kFull, best, off);
+            const int ow = __shfl_xor_sync(kFull, who, off);
+            if (ob < best) {
+                best = ob;
+                who = ow;
+            }
+        }
+        last = best;
+        const int b = target[who];
+        int hit = -1;
+        for (int k0 = 0; k0 < cnt && hit < 0; k0 += 32) {
+            const int k = k0 + lane;
+            const unsigned m = __ballot_sync(kFull, k < cnt && row[k] == b);
+            if (m) hit = k0 + __ffs(m) - 1;
+        }
+        if (hit >= 0) {
+            if (lane == 0) {
+                row[hit] = row[cnt - 1];
+                row[cnt - 1] = -1;
+            }
+            --cnt;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) n_neigh[i] = cnt;
+}
+
 }  // namespace
 }  // namespace pp
 
@@ -223,5 +327,31 @@ extern "C" int pp_neighbour_rows(const double* coords, int32_t nnodes, double ho
              static_cast<cudaStream_t>(stream)>>>(coords, nnodes, horizon * horizon,
                                                    lo3, 1.0 / cell, d3, cell_start, order,
                                                    width, nlist, family, overflow);
+    return launch_status();
+}
+
+extern "C" int pp_create_crack(const int32_t* crack, int32_t npairs, int32_t nnodes,
+                               int32_t max_neigh, int32_t* nlist, int32_t* n_neigh,
+                               int32_t* scratch, int32_t* bad, void* stream) {
+    if (npairs < 0 || nnodes < 0 || max_neigh < 1) return PP_ERROR_INVALID_VALUE;
+    if ((int64_t)npairs > (INT32_MAX - 1) / 2) return PP_ERROR_TOO_LARGE;
+    if (nnodes == INT32_MAX) return PP_ERROR_TOO_LARGE;
+    if (npairs == 0) return PP_SUCCESS;
+    if (!crack || !nlist || !n_neigh || !scratch || !bad) return PP_ERROR_INVALID_VALUE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // scratch: cs (nnodes + 1), then key and target (2 npairs each)
+    int32_t* cs = scratch;
+    int32_t* key = cs + (int64_t)nnodes + 1;
+    int32_t* target = key + 2 * (int64_t)npairs;
+    if (cudaMemsetAsync(cs, 0, ((size_t)nnodes + 1) * sizeof(int32_t), st) != cudaSuccess ||
+        cudaMemsetAsync(bad, 0, sizeof(int32_t), st) != cudaSuccess)
+        return PP_ERROR_CUDA;
+    const unsigned blocks = (unsigned)((npairs + 255) / 256);
+    k_crack_count<<<blocks, 256, 0, st>>>(crack, npairs, nnodes, cs, bad);
+    if (nnodes > 0) k_cell_scan<<<1, 1024, 0, st>>>(cs, nnodes);
+    k_crack_fill<<<blocks, 256, 0, st>>>(crack, npairs, nnodes, cs, bad, key, target);
+    if (nnodes > 0)
+        k_crack_apply<<<(nnodes + kRowWarps - 1) / kRowWarps, kRowWarps * 32, 0, st>>>(
+            nnodes, max_neigh, 2 * npairs, cs, bad, key, target, nlist, n_neigh);
     return launch_status();
 }

@@ -83,15 +83,20 @@ def plane_crack_pairs(coords, nlist, n_neigh, x0, y_max, axis=0,
     return np.stack([i[sel], j[sel]], axis=1)
 
 
-def remove_pairs(pairs, nlist, n_neigh):
-    """Vectorised ``create_crack`` for many pairs.
+def remove_pairs(pairs, nlist, n_neigh, context=None):
+    """``create_crack`` for many pairs: on the GPU of ``context`` when one
+    is given (:func:`.neighbours.create_crack`), else on the host.
 
-    Produces the same final neighbour list as applying
-    ``peripy/create_crack.pyx`` pair by pair when each row's removals are
-    applied in pair order: the row is compacted with the swap-remove rule.
+    Both produce the neighbour list of applying ``peripy/create_crack.pyx``
+    pair by pair: each row is compacted with the swap-remove rule in pair
+    order.
     """
-    from .model import create_crack
-    create_crack(pairs, nlist, n_neigh)
+    if context:
+        from .neighbours import create_crack as crack_on_gpu
+        crack_on_gpu(pairs, nlist, n_neigh, context)
+    else:
+        from .model import create_crack
+        create_crack(pairs, nlist, n_neigh)
 
 
 def face_bcs(coords, axis=0, tol=None):

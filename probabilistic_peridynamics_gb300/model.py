@@ -12,7 +12,8 @@ all outside the time step:
   ``scipy.spatial.cKDTree.query_pairs`` otherwise, instead of
   ``sklearn.neighbors.KDTree.query_radius`` (``model.py:564-566``); the
   neighbour *sets* are the same (distance <= horizon), rows are in
-  ascending node order;
+  ascending node order; the initial crack is cut on the same GPU
+  (``pp_create_crack``) with the reference's swap-remove result;
 * ``write_path`` caches arrays as ``.npy`` files instead of HDF5;
 * the stiffness-correction algorithms (``correction.pyx``) run on the GPU
   of the CUDA integrator (:mod:`.corrections`).
@@ -345,9 +346,10 @@ class Model(object):
                             initial_crack=None, context=None):
         """Family, neighbour list and crack (``peripy/model.py:536-597``).
 
-        With a CUDA integrator the families are built on its GPU
-        (:func:`.neighbours.neighbour_family`), else on the host; both give
-        the same rows.
+        With a CUDA integrator the families are built and the initial crack
+        is cut on its GPU (:func:`.neighbours.neighbour_family`,
+        :func:`.neighbours.create_crack`), else on the host; both give the
+        same rows.
         """
         if context:
             from .neighbours import neighbour_family
@@ -361,8 +363,13 @@ class Model(object):
         if initial_crack is not None:
             if callable(initial_crack):
                 initial_crack = initial_crack(coords, nlist, n_neigh)
-            create_crack(np.array(initial_crack, dtype=np.int32), nlist,
-                         n_neigh)
+            if context:
+                from .neighbours import create_crack as crack_on_gpu
+                crack_on_gpu(np.array(initial_crack, dtype=np.int32), nlist,
+                             n_neigh, context)
+            else:
+                create_crack(np.array(initial_crack, dtype=np.int32), nlist,
+                             n_neigh)
         return (family, nlist, n_neigh, max_neighbours)
 
     def _volume(self, transfinite, volume_total):

@@ -110,3 +110,85 @@ def neighbour_family(coords, horizon, context=None, pow2=True,
     compact = np.ascontiguousarray(nlist_h[:, :fmax])
     compact[compact == -1] = 0
     return family_h, compact, np.intc(fmax)
+
+
+def crack_device(crack, nlist, n_neigh, context):
+    """Apply ``pp_create_crack`` to device tensors in place.
+
+    :arg crack: ``(npairs, 2)`` int32 tensor of node indices in
+        ``[-nnodes, nnodes)`` on the context's device (see
+        :func:`create_crack` for negative ones).
+    :arg nlist: ``(nnodes, max_neigh)`` int32 device tensor, in/out.
+    :arg n_neigh: ``(nnodes,)`` int32 device tensor, in/out.
+    :raises IndexError: a node index is out of range (nothing is changed).
+    """
+    import torch
+    npairs = int(crack.shape[0])
+    if npairs == 0:
+        return
+    n, width = nlist.shape
+    for t in (crack, nlist, n_neigh):
+        if t.dtype != torch.int32 or not t.is_contiguous():
+            raise TypeError("crack, nlist and n_neigh must be contiguous "
+                            "int32 tensors")
+    dev = context.device
+    with context.on_stream():
+        scratch = torch.empty(n + 1 + 4 * npairs, dtype=torch.int32,
+                              device=dev)
+        bad = torch.empty(1, dtype=torch.int32, device=dev)
+        check(lib().pp_create_crack(crack.data_ptr(), npairs, n, width,
+                                    nlist.data_ptr(), n_neigh.data_ptr(),
+                                    scratch.data_ptr(), bad.data_ptr(),
+                                    context.stream_handle),
+              "pp_create_crack")
+        if int(bad.item()) != 0:
+            raise IndexError("crack node index out of range")
+
+
+def create_crack(crack, nlist, n_neigh, context=None):
+    """``peripy.create_crack.create_crack`` on the GPU: remove the bond pairs
+    in ``crack`` from the host arrays ``nlist`` and ``n_neigh`` in place.
+
+    Same result as the sequential loop of ``peripy/create_crack.pyx:1-43``:
+    for each pair ``(i, j)`` in order, ``j`` is removed from row ``i`` and
+    then ``i`` from row ``j``; a removed entry takes the row's last entry,
+    whose slot becomes ``-1``.  As with the reference's memoryviews, a
+    negative index selects the row counted from the end, but the node
+    looked for in the other row is the index as given, which no row holds.
+    At the first pair with an index outside ``[-nnodes, nnodes)`` the pairs
+    before it are applied and :class:`IndexError` is raised, as the
+    reference's bounds check does.
+
+    :arg crack: ``(npairs, 2)`` node indices.
+    :arg nlist: ``(nnodes, max_neigh)`` int32 C-contiguous host array.
+    :arg n_neigh: ``(nnodes,)`` int32 host array.
+    :arg context: a :class:`~.integrators.CUDAContext` (default: device 0).
+    """
+    import torch
+    from .integrators import CUDAContext
+    for name, a, nd in (("nlist", nlist, 2), ("n_neigh", n_neigh, 1)):
+        if (not isinstance(a, np.ndarray) or a.dtype != np.intc
+                or a.ndim != nd or not a.flags.c_contiguous
+                or not a.flags.writeable):
+            raise TypeError(f"{name} must be a writeable C-contiguous "
+                            f"int32 array of {nd} dimensions")
+    crack = np.asarray(crack, dtype=np.int64).reshape(-1, 2)
+    n = nlist.shape[0]
+    if n_neigh.shape[0] != n:
+        raise ValueError("nlist and n_neigh disagree on the number of nodes")
+    bad = np.nonzero(((crack < -n) | (crack >= n)).any(axis=1))[0]
+    stop = int(bad[0]) if bad.size else len(crack)
+    if stop:
+        ctx = context if context is not None else CUDAContext(0)
+        dev = ctx.device
+        with ctx.on_stream():
+            c = torch.as_tensor(
+                np.ascontiguousarray(crack[:stop], dtype=np.int32),
+                device=dev)
+            nl = torch.as_tensor(nlist, device=dev)
+            nn = torch.as_tensor(n_neigh, device=dev)
+            crack_device(c, nl, nn, ctx)
+            nlist[...] = nl.cpu().numpy()
+            n_neigh[...] = nn.cpu().numpy()
+    if bad.size:
+        raise IndexError("Out of bounds on buffer access (axis 0)")
