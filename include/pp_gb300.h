@@ -334,6 +334,55 @@ int pp_create_crack(const int32_t* crack, int32_t npairs, int32_t nnodes, int32_
                     void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Write-step sums.  Replace the NumPy reductions Model.simulate runs at    */
+/* every write (peripy/model.py:1320-1366), so that a write needs to copy   */
+/* back only u and damage (the mesh file's fields).                         */
+/*   pp_pairwise_plan (host only, no CUDA call) writes the summation tree   */
+/*     of NumPy's float64 sum of n contiguous elements (pairwise: leaves of */
+/*     at most 128 elements summed with eight running sums, split at n / 2  */
+/*     rounded down to a multiple of 8) into plan: [0] leaves, [1] inner    */
+/*     nodes, [2] heights, [3] n, then leaf first elements and lengths,     */
+/*     inner left and right value indices (leaves first, then inner nodes   */
+/*     by height) and height offsets.  Returns the plan's length in int32;  */
+/*     with plan NULL or capacity too small nothing is written; -1 when n   */
+/*     is outside [0, 2^31).                                               */
+/*   pp_write_sums computes, bit-identical to NumPy on the same arrays,     */
+/*     sums[0..5] = np.sum of u, ud, udd, force * volume[:, None],          */
+/*     body_force * volume[:, None] and damage, and for tip type t          */
+/*     sums[6 + 5 t + q] = the sequential sum from 0.0 over its (node, dof) */
+/*     entries of u, ud, udd, force * volume[node], body_force *            */
+/*     volume[node] (q = 0..4).  A NULL ud, udd, force or body_force counts */
+/*     as zeros (so do all arrays when nnodes is 0).  plan3 / plan1: device */
+/*     copies of the plans of 3 nnodes and                                  */
+/*     nnodes elements; scratch: 5 values3 + values1 doubles on the device. */
+/* ------------------------------------------------------------------------ */
+
+typedef struct pp_write_sums_args {
+    int32_t nnodes;
+    int32_t ntips;                 /* tip types                            */
+    int32_t leaves3;               /* plan3[0]                             */
+    int32_t values3;               /* plan3[0] + plan3[1]                  */
+    int32_t leaves1;               /* plan1[0]                             */
+    int32_t values1;               /* plan1[0] + plan1[1]                  */
+    const double* u;               /* (nnodes, 3)                          */
+    const double* ud;              /* (nnodes, 3) or NULL                  */
+    const double* udd;             /* (nnodes, 3) or NULL                  */
+    const double* force;           /* (nnodes, 3) or NULL                  */
+    const double* body_force;      /* (nnodes, 3) or NULL                  */
+    const double* damage;          /* (nnodes)                             */
+    const double* volume;          /* (nnodes)                             */
+    const int32_t* plan3;          /* pp_pairwise_plan(3 nnodes)           */
+    const int32_t* plan1;          /* pp_pairwise_plan(nnodes)             */
+    const int32_t* tip_offsets;    /* (ntips + 1) into tip_entries         */
+    const int32_t* tip_entries;    /* (tip_offsets[ntips], 2) node, dof    */
+    double* scratch;               /* 5 values3 + values1                  */
+    double* sums;                  /* (6 + 5 ntips) out                    */
+} pp_write_sums_args;
+
+int64_t pp_pairwise_plan(int64_t n, int32_t* plan, int64_t capacity);
+int pp_write_sums(const pp_write_sums_args* args, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Stiffness correction factors (set-up).  Replaces the correction          */
 /* algorithms of peripy/correction.pyx:5-277 as Model.__init__ applies them */
 /* (peripy/model.py:349-375, 782-935): each selected factor multiplies the  */

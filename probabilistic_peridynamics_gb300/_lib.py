@@ -96,6 +96,18 @@ class CorrectionsArgs(ctypes.Structure):
     ]
 
 
+class WriteSumsArgs(ctypes.Structure):
+    """Mirror of ``pp_write_sums_args``."""
+    _fields_ = [
+        ("nnodes", _i32), ("ntips", _i32), ("leaves3", _i32),
+        ("values3", _i32), ("leaves1", _i32), ("values1", _i32),
+        ("u", _vp), ("ud", _vp), ("udd", _vp), ("force", _vp),
+        ("body_force", _vp), ("damage", _vp), ("volume", _vp),
+        ("plan3", _vp), ("plan1", _vp), ("tip_offsets", _vp),
+        ("tip_entries", _vp), ("scratch", _vp), ("sums", _vp),
+    ]
+
+
 class AdjointArgs(ctypes.Structure):
     """Mirror of ``pp_adjoint_args``."""
 
@@ -135,6 +147,8 @@ SIGNATURES = {
                                          _vp, _i32, _vp, _vp, _vp, _vp]),
     "pp_create_crack": (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp, _vp, _vp,
                                        _vp, _vp]),
+    "pp_pairwise_plan": (ctypes.c_int64, [_i64, _vp, _i64]),
+    "pp_write_sums": (ctypes.c_int, [ctypes.POINTER(WriteSumsArgs), _vp]),
     "pp_mixed_pack": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
     "pp_mixed_export": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
     "pp_partner_slots": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp]),

@@ -599,7 +599,8 @@ class _CUDAIntegrator(Integrator):
             return self._write(u, ud, udd, force, body_force, damage, nlist,
                                n_neigh)
 
-    def _write(self, u, ud, udd, force, body_force, damage, nlist, n_neigh):
+    def _synced(self):
+        """Export the state and damage, and check the device status."""
         self._sync_state()
         self.context.stream.synchronize()
         if self.precision == "mixed":
@@ -608,16 +609,38 @@ class _CUDAIntegrator(Integrator):
                 raise _lib.LibraryError(
                     f"a mixed-precision step reported device status {status} "
                     "(PP_STATUS_*): the state is invalid")
+
+    @staticmethod
+    def _put(host, dev):
+        src = dev.cpu().numpy()
+        if host is None:
+            return src
+        flat = host.reshape(-1)
+        flat[:src.size] = src.reshape(-1)[:flat.size]
+        return host
+
+    def write_sums(self, u, damage, sums):
+        """A write step that brings back only ``u`` and ``damage``.
+
+        Computes the damage, copies displacements and damage into the given
+        host arrays (as :meth:`write` does) and evaluates the write-step
+        sums of the whole state on the device.
+
+        :arg sums: a :class:`~.writes.WriteSums` of this model.
+        :returns: ``(u, damage, values)``, ``values`` as
+            :meth:`.writes.WriteSums.__call__` returns them.
+        """
+        with self.context.on_stream():
+            self._synced()
+            values = sums(self.u_d[self._parity], self.ud_d, self.udd_d,
+                          self.force_d, self.body_force_d, self.damage_d)
+            return (self._put(u, self.u_d[self._parity]),
+                    self._put(damage, self.damage_d), values)
+
+    def _write(self, u, ud, udd, force, body_force, damage, nlist, n_neigh):
+        self._synced()
         cur = self.u_d[self._parity]
-
-        def put(host, dev):
-            src = dev.cpu().numpy()
-            if host is None:
-                return src
-            flat = host.reshape(-1)
-            flat[:src.size] = src.reshape(-1)[:flat.size]
-            return host
-
+        put = self._put
         u = put(u, cur)
         ud = put(ud, self.ud_d)
         udd = put(udd, self.udd_d)
