@@ -84,13 +84,18 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--accuracy-steps", type=int, default=E2E_STEPS)
     p.add_argument("--workload",
-                   choices=["large", "batched", "composite", "adjoint"],
+                   choices=["large", "batched", "composite", "adjoint",
+                            "writes", "setup"],
                    default="large",
                    help="large: the 200x200x10 Velocity-Verlet plate (the "
                         "headline); batched: 64 uneven UQ instances, "
                         "Euler-Cromer; composite: 1M Poisson-disk points, "
                         "three bond types, trilinear damage; adjoint: "
-                        "forward + backward passes of the 50x50x5 rollout")
+                        "forward + backward passes of the 50x50x5 rollout; "
+                        "writes: Model.simulate of the plate with a write "
+                        "every 500 steps, device sums against host copies; "
+                        "setup: neighbour families and initial crack of the "
+                        "plate, GPU against host and the reference")
     p.add_argument("--profile", choices=["mixed", "fp64", "plain"],
                    help="only run 3 warm-up and 3 profiled launches of one "
                         "step variant on the full workload (for ncu)")
@@ -766,6 +771,188 @@ def adjoint_main(args):
     print(json.dumps(line), flush=True)
 
 
+def writes_main(args):
+    """Model.simulate on the 200x200x10 plate with a write every 500 of
+    5000 Velocity-Verlet steps (mixed precision): mesh files of u and damage
+    plus the recorded sums, with one tip type (the x dof of the pulled
+    x-max face).  Timed twice through the public API: with the write-step
+    sums on the device (only u and damage come back) and with the host path
+    that copies all eight state arrays back at every write (the reference's
+    Integrator.write), both writing the same files and data."""
+    import torch
+    import warnings
+    import probabilistic_peridynamics_gb300 as pp
+    from probabilistic_peridynamics_gb300.mesh import write_vtk
+    w = build_workload()
+    steps, every = E2E_STEPS, 500
+    tmp = tempfile.mkdtemp()
+    mesh = os.path.join(tmp, "lattice.vtk")
+    write_vtk(mesh, w["coords"], [])
+    lo, hi = w["coords"][:, 0].min(), w["coords"][:, 0].max()
+
+    def is_bnd(x):
+        if x[0] <= lo + 1e-9:
+            return [-1.0, None, None]
+        if x[0] >= hi - 1e-9:
+            return [1.0, None, None]
+        return [None, None, None]
+
+    def is_tip(x):
+        return ["pulled", None, None] if x[0] >= hi - 1e-9 else \
+            [None, None, None]
+
+    class HostWrites(pp.VelocityVerletCUDA):
+        write_sums = None
+
+    mags = PULL_RATE * np.arange(1, steps + 1)
+    out = {}
+    for name, cls in (("device_sums", pp.VelocityVerletCUDA),
+                      ("host_copies", HostWrites)):
+        integ = cls(DAMPING, dt=DT, precision="mixed")
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            model = pp.Model(mesh, integ, horizon=w["horizon"],
+                             critical_stretch=S0, bond_stiffness=w["k"],
+                             transfinite=1,
+                             volume_total=float(w["volume"].sum()),
+                             connectivity=(w["nlist"], w["n_neigh"]),
+                             family=w["family"], dimensions=3,
+                             density=np.full(w["nnodes"], DENSITY),
+                             is_displacement_boundary=is_bnd, is_tip=is_tip)
+        path = pathlib.Path(tmp) / name
+        path.mkdir()
+        model.simulate(steps=20, displacement_bc_magnitudes=mags, write=10,
+                       write_path=path)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = model.simulate(steps=steps, displacement_bc_magnitudes=mags,
+                             write=every, write_path=path)
+        torch.cuda.synchronize()
+        out[name] = (time.perf_counter() - t0, res[5])
+        del model, integ
+        torch.cuda.empty_cache()
+    dev_s, dev_data = out["device_sums"]
+    host_s, host_data = out["host_copies"]
+    same = all(np.array_equal(dev_data[k][f], host_data[k][f])
+               for k in host_data for f in host_data[k])
+    n = w["nnodes"]
+    nwrites = steps // every
+    line = {
+        "metric": "bond-updates/s through Model.simulate with writes",
+        "value": w["bonds"] * steps / dev_s, "unit": UNIT, "n_gpus": 1,
+        "steps": steps, "warmup": 20, "ms_per_step": 1e3 * dev_s / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD + f"; write every {every} steps "
+                               "(mesh file + recorded sums), one tip type",
+                   "writes": nwrites, "nodes": n, "bonds": w["bonds"]},
+        "variants": {
+            "device_sums": {"wall_s": dev_s,
+                            "d2h_bytes_per_write": n * 24 + n * 8},
+            "host_copies": {"wall_s": host_s,
+                            "d2h_bytes_per_write":
+                                5 * n * 24 + n * 8 + w["nlist"].nbytes
+                                + w["n_neigh"].nbytes,
+                            "value": w["bonds"] * steps / host_s}},
+        "data_identical": bool(same),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def setup_main(args):
+    """Model set-up of the 200x200x10 plate on the GPU: neighbour families
+    (cell search) and the plane crack (30,940 pairs, pp_create_crack), each
+    timed on device-resident arrays (CUDA events, median of --steps runs
+    after --warmup) and through the host-array entry points; beside them
+    the host search (scipy cKDTree pairs assembled into rows) and the
+    reference's own compiled create_crack on one core, all on the same
+    arrays and checked equal."""
+    import torch
+    from probabilistic_peridynamics_gb300 import lattice
+    from probabilistic_peridynamics_gb300.integrators import CUDAContext
+    from probabilistic_peridynamics_gb300.model import (build_family,
+                                                        neighbour_pairs)
+    from probabilistic_peridynamics_gb300.neighbours import (
+        crack_device, create_crack, neighbour_family)
+    ctx = CUDAContext(0)
+    coords = lattice.lattice_coords(NX, NY, NZ, DX)
+    horizon = HORIZON_CELLS * DX
+    family, nlist, _ = neighbour_family(coords, horizon, ctx)
+    t0 = time.perf_counter()
+    family, nlist, _ = neighbour_family(coords, horizon, ctx)
+    nb_gpu_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    fam_h, nl_h, _ = build_family(coords.shape[0],
+                                  neighbour_pairs(coords, horizon))
+    nb_host_s = time.perf_counter() - t0
+    same_rows = bool(np.array_equal(family, fam_h)
+                     and np.array_equal(nlist, nl_h))
+    n_neigh = family.copy()
+    pairs = np.ascontiguousarray(
+        lattice.plane_crack_pairs(coords, nlist, n_neigh, 0.5, 0.25),
+        dtype=np.intc)
+    dev = ctx.device
+    with ctx.on_stream():
+        nl_d = torch.as_tensor(nlist, device=dev)
+        nn_d = torch.as_tensor(n_neigh, device=dev)
+        c_d = torch.as_tensor(pairs, device=dev)
+        times = []
+        for k in range(max(args.warmup, 1) + max(args.steps, 1)):
+            x, y = nl_d.clone(), nn_d.clone()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ctx.stream)
+            crack_device(c_d, x, y, ctx)
+            e1.record(ctx.stream)
+            e1.synchronize()
+            if k >= max(args.warmup, 1):
+                times.append(e0.elapsed_time(e1))
+    crack_dev_ms = statistics.median(times)
+    got_nl, got_nn = nlist.copy(), n_neigh.copy()
+    t0 = time.perf_counter()
+    create_crack(pairs, got_nl, got_nn, ctx)
+    crack_host_arrays_s = time.perf_counter() - t0
+    same_dev = bool(np.array_equal(x.cpu().numpy(), got_nl))
+    ref = reference_step_fn()
+    ref_s = None
+    same_ref = None
+    if ref is not None:
+        from oracle import build_ref
+        ref_crack = build_ref.load("create_crack").create_crack
+        r_nl, r_nn = nlist.copy(), n_neigh.copy()
+        t0 = time.perf_counter()
+        ref_crack(pairs, r_nl, r_nn)
+        ref_s = time.perf_counter() - t0
+        same_ref = bool(np.array_equal(r_nl, got_nl)
+                        and np.array_equal(r_nn, got_nn))
+    line = {
+        "metric": "initial-crack time on device-resident arrays",
+        "value": crack_dev_ms, "unit": "ms", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": crack_dev_ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic",
+        "config": {"workload": "set-up of the 200x200x10 lattice "
+                               "(400k nodes): neighbour families and the "
+                               "plane crack x = 0.5, y < 0.25",
+                   "crack_pairs": int(len(pairs)),
+                   "bonds": int(family.sum())},
+        "crack": {"device_ms": crack_dev_ms,
+                  "host_arrays_s": crack_host_arrays_s,
+                  "same_as_host_array_path": same_dev,
+                  "reference_compiled_s": ref_s,
+                  "same_as_reference": same_ref},
+        "neighbours": {"gpu_s": nb_gpu_s, "host_kdtree_s": nb_host_s,
+                       "same_rows": same_rows},
+        "cpu_baseline": ({"value": ref_s * 1e3, "unit": "ms", "cores": 1,
+                          "kind": "reference",
+                          "sample": "the reference's compiled "
+                                    "create_crack on the same crack list"}
+                         if ref_s is not None else None),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.profile:
@@ -782,6 +969,12 @@ def main():
         return
     if args.workload == "adjoint":
         adjoint_main(args)
+        return
+    if args.workload == "writes":
+        writes_main(args)
+        return
+    if args.workload == "setup":
+        setup_main(args)
         return
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))

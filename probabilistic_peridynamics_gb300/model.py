@@ -673,6 +673,11 @@ class Model(object):
         last = first_step + steps - 1
         bar = _progress(range(steps), desc="Simulation Progress",
                         unit="steps")
+        # A write with device sums leaves its mesh file and record pending
+        # until the next segment of steps is queued, so that the host writes
+        # the file while the GPU steps; it is finished before the next write
+        # refills u and damage.
+        pending = None
         while step <= last:
             if write:
                 nxt = min(last, ((step + write - 1) // write) * write)
@@ -686,6 +691,9 @@ class Model(object):
                 for s in range(step, nxt + 1):
                     self.integrator(displacement_bc_magnitudes[s - 1],
                                     force_bc_magnitudes[s - 1])
+            if pending is not None:
+                self._finish_write(data, nwrites, *pending)
+                pending = None
             step = nxt + 1
             if hasattr(bar, "update"):
                 bar.update(count)
@@ -694,8 +702,8 @@ class Model(object):
                 if sums is not None:
                     u, damage, values = self.integrator.write_sums(
                         u, damage, sums)
-                    self.write_mesh(write_path / f"U_{nxt}.vtk", damage, u)
-                    self._record_sums(data, ii, nxt, nwrites, values)
+                    pending = (write_path / f"U_{nxt}.vtk", u, damage, ii,
+                               nxt, values)
                     continue
                 (u, ud, udd, force, body_force, damage, nlist,
                  n_neigh) = self.integrator.write(
@@ -703,6 +711,8 @@ class Model(object):
                 self.write_mesh(write_path / f"U_{nxt}.vtk", damage, u)
                 self._record(data, ii, nxt, nwrites, u, ud, udd, force,
                              body_force, damage)
+        if pending is not None:
+            self._finish_write(data, nwrites, *pending)
         if hasattr(bar, "close"):
             bar.close()
         for tip_type_str in data:
@@ -749,6 +759,12 @@ class Model(object):
         if damage_sum > 0.05 * self.nnodes:
             warnings.warn('Over 5% of bonds have broken! peridynamics '
                           'simulation continuing')
+
+    def _finish_write(self, data, nwrites, path, u, damage, ii, step,
+                      values):
+        """Mesh file and record of a write with device sums."""
+        self.write_mesh(path, damage, u)
+        self._record_sums(data, ii, step, nwrites, values)
 
     def _record_sums(self, data, ii, step, nwrites, values):
         """:meth:`_record` from sums computed on the device
