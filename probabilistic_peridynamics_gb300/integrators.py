@@ -612,9 +612,24 @@ class _CUDAIntegrator(Integrator):
 
     @staticmethod
     def _put(host, dev):
-        src = dev.cpu().numpy()
+        """Fill ``host`` with ``dev`` (as ``cl.enqueue_copy`` fills it).
+
+        A C-contiguous, writeable host array of the device dtype and size
+        receives the copy directly (the DMA writes its pages; a fresh
+        staging array would be page-faulted in first, several times
+        slower); anything else goes through a host copy.
+        """
+        import torch
         if host is None:
-            return src
+            return dev.cpu().numpy()
+        np_dtype = {torch.float64: np.float64, torch.float32: np.float32,
+                    torch.int32: np.int32, torch.int64: np.int64}.get(dev.dtype)
+        if (isinstance(host, np.ndarray) and host.flags.c_contiguous
+                and host.flags.writeable and host.size == dev.numel()
+                and host.dtype == np_dtype):
+            torch.from_numpy(host.reshape(-1)).copy_(dev.reshape(-1))
+            return host
+        src = dev.cpu().numpy()
         flat = host.reshape(-1)
         flat[:src.size] = src.reshape(-1)[:flat.size]
         return host
