@@ -345,6 +345,25 @@ def e2e_simulate(w, torch):
                          is_displacement_boundary=is_bnd)
     mags = PULL_RATE * np.arange(1, E2E_STEPS + 1)
     model.simulate(steps=20, displacement_bc_magnitudes=mags)  # warm-up
+    # where the wall time goes: the integrator calls Model.simulate makes
+    # (each already ends in, or is followed by, a synchronisation)
+    parts = {}
+
+    def timed(name):
+        fn = getattr(integ, name)
+
+        def call(*a, **k):
+            t = time.perf_counter()
+            try:
+                return fn(*a, **k)
+            finally:
+                if name == "_run":
+                    torch.cuda.synchronize()
+                parts[name] = parts.get(name, 0.0) + time.perf_counter() - t
+        setattr(integ, name, call)
+
+    for name in ("create_buffers", "_run", "write"):
+        timed(name)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     u, damage, (nlist, n_neigh), force, ud, _ = model.simulate(
@@ -360,6 +379,10 @@ def e2e_simulate(w, torch):
             "h2d_bytes_per_step": h2d / E2E_STEPS,
             "d2h_bytes_per_step": d2h / E2E_STEPS,
             "steps": E2E_STEPS, "wall_s": dt_s,
+            "wall_parts_s": {"create_buffers": parts.get("create_buffers"),
+                             "steps": parts.get("_run"),
+                             "write": parts.get("write"),
+                             "rest": dt_s - sum(parts.values())},
             "path": "Model.simulate (VelocityVerletCUDA, precision='mixed')"}
 
 
