@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define PP_ABI_VERSION 1
+#define PP_ABI_VERSION 2
 
 /* Status codes. */
 #define PP_SUCCESS                  0
@@ -216,6 +216,10 @@ typedef struct pp_fused_args {
     const double* densities;       /* EC / VV                              */
     const double* stiffness_corrections;  /* or NULL                       */
     const int32_t* bond_types;     /* or NULL                              */
+    const double* bond_length;     /* PP_FLOAT64, optional: |r0[j] - r0[i]|
+                                      per slot (nnodes, max_neigh), written
+                                      by pp_bond_lengths; NULL: computed in
+                                      every step (the same binary64 value) */
     /* batched independent instances (PMB only): node i uses critical
        stretch instance_s0[node_instance[i]]; NULL = one model          */
     const int32_t* node_instance;  /* (nnodes) or NULL                     */
@@ -272,6 +276,14 @@ int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t nsteps,
  * The caller derives pos_scale and min_bond for PP_MIXED from them. */
 int pp_bond_extent(const int32_t* nlist, const double* r0, int32_t nnodes,
                    int32_t max_neigh, double* extent, void* stream);
+
+/* Reference bond lengths for PP_FLOAT64 (pp_fused_args.bond_length):
+ * length[i * max_neigh + k] = sqrt((x*x + y*y) + z*z) in binary64 with
+ * (x, y, z) = r0[j] - r0[i], j = nlist[i * max_neigh + k], the value the
+ * step computes for xi (peripy/cl/peridynamics.cl:65-73); 0 where j is -1.
+ * A length stays valid while nlist only loses bonds (set to -1). */
+int pp_bond_lengths(const double* r0, const int32_t* nlist, int32_t nnodes,
+                    int32_t max_neigh, double* length, void* stream);
 
 /* Builds the PP_MIXED layouts from the reference layouts: rec[parity] from
  * r0, vols (with args->pos_scale/pos_origin, which the caller chooses) and

@@ -70,7 +70,8 @@ class FusedArgs(ctypes.Structure):
         ("r0", _vp), ("vols", _vp), ("family", _vp), ("bc_types", _vp),
         ("bc_values", _vp), ("fc_types", _vp), ("fc_values", _vp),
         ("densities", _vp), ("stiffness_corrections", _vp),
-        ("bond_types", _vp), ("node_instance", _vp), ("instance_s0", _vp),
+        ("bond_types", _vp), ("bond_length", _vp), ("node_instance", _vp),
+        ("instance_s0", _vp),
         ("ninstances", _i32), ("reserved2", _i32),
         ("nlist", _vp), ("regimes", _vp),
         ("u", _vp * 2), ("ud", _vp), ("udd", _vp), ("force", _vp),
@@ -148,6 +149,7 @@ SIGNATURES = {
     "pp_create_crack": (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp, _vp, _vp,
                                        _vp, _vp]),
     "pp_pairwise_plan": (ctypes.c_int64, [_i64, _vp, _i64]),
+    "pp_bond_lengths": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
     "pp_write_sums": (ctypes.c_int, [ctypes.POINTER(WriteSumsArgs), _vp]),
     "pp_mixed_pack": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
     "pp_mixed_export": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),

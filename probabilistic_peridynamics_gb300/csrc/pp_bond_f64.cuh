@@ -29,6 +29,7 @@ struct F64Bond {
     const double* ktab;
     const double* stab;
     const double* ctab;
+    const double* xi_len;     // per-slot |xi| (pp_bond_lengths) or nullptr
     double k;
     double s0;
     int nregimes;
@@ -49,7 +50,10 @@ __device__ __forceinline__ d3 f64_slot(const F64Bond& b, int64_t gid, d3 ri, d3 
     const double xe_x = dadd(dsub(uj[0], ui.x), xi_x);
     const double xe_y = dadd(dsub(uj[1], ui.y), xi_y);
     const double xe_z = dadd(dsub(uj[2], ui.z), xi_z);
-    const double xi = dsqrt(dadd(dadd(dmul(xi_x, xi_x), dmul(xi_y, xi_y)), dmul(xi_z, xi_z)));
+    // |xi| never changes: read it when cached (the same binary64 value)
+    const double xi = b.xi_len ? b.xi_len[gid]
+                               : dsqrt(dadd(dadd(dmul(xi_x, xi_x), dmul(xi_y, xi_y)),
+                                            dmul(xi_z, xi_z)));
     const double y = dsqrt(dadd(dadd(dmul(xe_x, xe_x), dmul(xe_y, xe_y)), dmul(xe_z, xe_z)));
     const double s = ddiv(dsub(y, xi), xi);
     double f;

@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(256) k_fused_f64(pp_fused_args a, int parity, 
                         a.bond_stiffness_table,
                         a.critical_stretch_table,
                         a.plus_cs,
+                        a.bond_length,
                         a.bond_stiffness,
                         a.node_instance ? a.instance_s0[a.node_instance[i]] : a.critical_stretch,
                         a.nregimes};
@@ -103,6 +104,23 @@ __global__ void __launch_bounds__(256) k_fused_f64(pp_fused_args a, int parity, 
             a.damage[n] = damage_of(count, a.family[n]);
         }
     }
+}
+
+// One thread per slot: |r0[j] - r0[i]| as the bond body computes it.
+__global__ void k_bond_lengths(const double* __restrict__ r0, const int32_t* __restrict__ nlist,
+                               int nnodes, int max_neigh, double* __restrict__ length) {
+    const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= (int64_t)nnodes * max_neigh) return;
+    const int j = nlist[g];
+    const int64_t i = g / max_neigh;
+    double len = 0.0;
+    if (j >= 0 && j < nnodes) {
+        const double x = dsub(r0[3 * (int64_t)j], r0[3 * i]);
+        const double y = dsub(r0[3 * (int64_t)j + 1], r0[3 * i + 1]);
+        const double z = dsub(r0[3 * (int64_t)j + 2], r0[3 * i + 2]);
+        len = dsqrt(dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z)));
+    }
+    length[g] = len;
 }
 
 __global__ void k_set_base(int64_t* base, int64_t v) { *base = v; }
@@ -244,4 +262,16 @@ extern "C" int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t n
         p ^= 1;
     }
     return PP_SUCCESS;
+}
+
+extern "C" int pp_bond_lengths(const double* r0, const int32_t* nlist, int32_t nnodes,
+                               int32_t max_neigh, double* length, void* stream) {
+    if (nnodes < 0) return PP_ERROR_INVALID_VALUE;
+    if (!is_pow2_le_1024(max_neigh)) return PP_ERROR_MAX_NEIGH;
+    if (nnodes == 0) return PP_SUCCESS;
+    if (!r0 || !nlist || !length) return PP_ERROR_INVALID_VALUE;
+    const int64_t slots = (int64_t)nnodes * max_neigh;
+    k_bond_lengths<<<(unsigned)((slots + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        r0, nlist, nnodes, max_neigh, length);
+    return launch_status();
 }

@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                     a.bond_stiffness_table,
                     a.critical_stretch_table,
                     a.plus_cs,
+                    nullptr,  // the plain step recomputes |xi| as the reference does
                     a.bond_stiffness,
                     a.critical_stretch,
                     a.nregimes};

@@ -389,6 +389,16 @@ class _CUDAIntegrator(Integrator):
         self._parity = 0
         if self.precision == "mixed":
             self._create_mixed_buffers()
+        self.bond_length_d = None
+        if self.fused and self.precision == "float64":
+            # |xi| per slot, read by the fused binary64 step instead of a
+            # square root per bond and step (the same binary64 value)
+            self.bond_length_d = torch.empty(
+                (n, self.max_neighbours), dtype=torch.float64,
+                device=self.context.device)
+            check(lib().pp_bond_lengths(
+                _ptr(self.r0_d), _ptr(self.nlist_d), n, self.max_neighbours,
+                _ptr(self.bond_length_d), self._stream), "pp_bond_lengths")
         self._fargs = self._make_fused_args() if self.fused else None
         if self.precision == "mixed":
             check(lib().pp_mixed_pack(ctypes.byref(self._fargs), 0,
@@ -454,6 +464,7 @@ class _CUDAIntegrator(Integrator):
         a.densities = _ptr(self.densities_d)
         a.stiffness_corrections = _ptr(self.stiffness_corrections_d)
         a.bond_types = _ptr(self.bond_types_d)
+        a.bond_length = _ptr(getattr(self, "bond_length_d", None))
         if self.node_instance_d is not None:
             a.node_instance = _ptr(self.node_instance_d)
             a.instance_s0 = _ptr(self.instance_s0_d)

@@ -43,7 +43,7 @@ def test_header_functions_exported(L):
 
 
 def test_abi_version_and_status_strings(L):
-    assert L.pp_abi_version() == 1
+    assert L.pp_abi_version() == 2
     assert L.pp_status_string(0) == b"success"
     assert b"power of two" in L.pp_status_string(2)
 
@@ -59,6 +59,7 @@ def test_struct_layout_matches_header():
     assert f["variant"].offset == 32
     assert f["dt"].offset == 40
     assert f["bond_stiffness_table"].offset == 72
+    assert f["bond_length"].offset == f["bond_types"].offset + 8
     assert f["pos_origin"].offset + 24 == ctypes.sizeof(_lib.FusedArgs)
     # pp_corrections_args: 6 int32, 5 doubles, 6 pointers
     assert ctypes.sizeof(_lib.CorrectionsArgs) == 6 * 4 + 5 * 8 + 6 * 8
@@ -118,6 +119,17 @@ def test_validation_without_gpu(L):
     fa.pos_scale = 1.0
     assert L.pp_fused_step(ctypes.byref(fa), 0, 0.0, 0.0, None) == \
         _lib.PP_ERROR_MISALIGNED
+
+
+def test_bond_lengths_validation_without_gpu(L):
+    from probabilistic_peridynamics_gb300 import _lib
+    assert L.pp_bond_lengths(None, None, 10, 3, None, None) == \
+        _lib.PP_ERROR_MAX_NEIGH
+    assert L.pp_bond_lengths(None, None, 0, 4, None, None) == _lib.PP_SUCCESS
+    assert L.pp_bond_lengths(None, None, 10, 4, None, None) == \
+        _lib.PP_ERROR_INVALID_VALUE
+    assert L.pp_bond_lengths(None, None, -1, 4, None, None) == \
+        _lib.PP_ERROR_INVALID_VALUE
 
 
 def test_fixed_point_frame_exact_differences():
