@@ -96,7 +96,8 @@ def parse_args():
                         "every 500 steps, device sums against host copies; "
                         "setup: neighbour families and initial crack of the "
                         "plate, GPU against host and the reference")
-    p.add_argument("--profile", choices=["mixed", "fp64", "plain"],
+    p.add_argument("--profile", choices=["mixed", "fp64", "plain",
+                                         "composite"],
                    help="only run 3 warm-up and 3 profiled launches of one "
                         "step variant on the full workload (for ncu)")
     return p.parse_args()
@@ -105,6 +106,9 @@ def parse_args():
 def profile_case(which):
     """3 warm-up + 3 launches of one step variant, direct launches."""
     import torch
+    if which == "composite":
+        profile_composite()
+        return
     w = build_workload()
     precision = "mixed" if which == "mixed" else "float64"
     integ = make_integrator(w, precision, which != "plain", autotune=False)
@@ -115,6 +119,32 @@ def profile_case(which):
     integ.context.stream.synchronize()
     torch.cuda.synchronize()
     print(f"profile case {which}: 6 steps done", flush=True)
+
+
+def profile_composite():
+    """3 warm-up + 3 launches of the composite's mixed step (compensated
+    sums, the tile shape of PP_PROFILE_VARIANT, default 2)."""
+    import torch
+    import probabilistic_peridynamics_gb300 as pp
+    from probabilistic_peridynamics_gb300.integrators import CUDAContext
+    from probabilistic_peridynamics_gb300.pointset import composite
+    w = composite(context=CUDAContext(0))
+    n = w["coords"].shape[0]
+    integ = pp.VelocityVerletCUDA(DAMPING, dt=DT, precision="mixed",
+                                  compensated=True, autotune=False)
+    integ.build(n, 3, w["max_neigh"], w["coords"], w["volume"], w["family"],
+                w["bc_types"], w["bc_values"], np.zeros((n, 3), dtype=np.intc),
+                np.zeros((n, 3)), None, w["bond_types"], w["densities"])
+    z = np.zeros((n, 3))
+    integ.create_buffers(w["nlist"], w["n_neigh"], w["bond_stiffness"],
+                         w["critical_stretch"], w["plus_cs"], z, z, z, z, z,
+                         np.zeros(n), None, w["nregimes"], w["nbond_types"])
+    integ._fargs.variant = int(os.environ.get("PP_PROFILE_VARIANT", "2"))
+    for k in range(6):
+        integ(COMPOSITE_RATE * (k + 1), 0.0)
+    integ.context.stream.synchronize()
+    torch.cuda.synchronize()
+    print("profile case composite: 6 steps done", flush=True)
 
 
 # ----------------------------------------------------------------- workload
