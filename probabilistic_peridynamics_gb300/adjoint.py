@@ -82,6 +82,13 @@ class AdjointProblem:
             check(lib().pp_partner_slots(_p(self.nlist0), n, mn,
                                          _p(self.partner), self._stream),
                   "pp_partner_slots")
+            # reference bond lengths for the binary64 forward step (read
+            # instead of a square root per bond and step; same values)
+            self.bond_length = torch.empty((n, mn), dtype=torch.float64,
+                                           device=dev)
+            check(lib().pp_bond_lengths(_p(self.r0), _p(self.nlist0), n, mn,
+                                        _p(self.bond_length), self._stream),
+                  "pp_bond_lengths")
 
     @property
     def _stream(self):
@@ -105,6 +112,7 @@ class AdjointProblem:
         a.bc_types, a.bc_values = _p(self.bc_types), _p(self.bc_values)
         a.fc_types, a.fc_values = _p(self.zeros_i), _p(self.zeros_d)
         a.stiffness_corrections = _p(k)
+        a.bond_length = _p(self.bond_length)
         a.nlist = _p(nlist)
         a.u[0], a.u[1] = u.data_ptr(), out.data_ptr()
         a.force, a.body_force = _p(self.force), _p(self.body)
