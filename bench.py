@@ -321,6 +321,41 @@ def time_plain_steps(integ, steps, warmup, torch):
     return e0.elapsed_time(e1) / steps
 
 
+def time_cython_euler(w, steps, torch):
+    """PeriPy's CPU integrator ``Euler`` on the GPU (``pp.Euler``: the
+    Cython step's semantics and results) on the bench lattice in its compact
+    layout, with the CPU samples' Euler dt: the like-for-like counterpart of
+    the reference CPU step that ``cpu_baseline`` times."""
+    import probabilistic_peridynamics_gb300 as pp
+    n = w["nnodes"]
+    nl = compact(w["nlist"], w["family"])
+    it = pp.Euler(CPU_DT)
+    it.build(n, 3, nl.shape[1], w["coords"], w["volume"], w["family"],
+             w["bc_types"], w["bc_values"], w["force_bc_types"],
+             w["force_bc_values"], None, None, None)
+    z = np.zeros((n, 3))
+    it.create_buffers(nl, w["n_neigh"].copy(), w["k"], S0, None, z.copy(),
+                      z.copy(), z.copy(), z.copy(), z.copy(), np.zeros(n),
+                      None, 1, 1)
+    stream = it.device_context.stream
+    for k in range(2):
+        it(PULL_RATE * (k + 1), 0.0)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(steps):
+        it(PULL_RATE * (k + 3), 0.0)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    del it
+    torch.cuda.empty_cache()
+    return {"bond_updates_per_s": w["bonds"] / (ms * 1e-3),
+            "ms_per_step": ms, "dt": CPU_DT,
+            "layout": "compact rows (width family.max())"}
+
+
 def accuracy(w, steps, torch):
     """Mixed vs FP64 fused (bit-identical to the plain FP64 step) after
     ``steps`` steps from the same state: displacement error and mask."""
@@ -1086,6 +1121,8 @@ def main():
         torch.cuda.empty_cache()
     variants["speedup_mixed_vs_plain_fp64"] = (
         value / variants["plain_fp64"]["bond_updates_per_s"])
+    variants["euler_cython_gpu"] = time_cython_euler(w, args.fp64_steps,
+                                                     torch)
 
     acc = accuracy(w, args.accuracy_steps, torch) if args.accuracy_steps \
         else None

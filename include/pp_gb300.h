@@ -346,6 +346,40 @@ int pp_create_crack(const int32_t* crack, int32_t npairs, int32_t nnodes, int32_
                     void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* PeriPy's CPU integrator `Euler` (peripy/integrators.py:303-459) on the   */
+/* GPU: the arithmetic and the sequential semantics of the Cython module     */
+/* peripy/peridynamics.pyx, bit for bit.  Layout: the compact neighbour list */
+/* `Model` builds without a device context ((nnodes, max_neigh) int32, the   */
+/* first n_neigh[i] entries of row i valid, max_neigh = family.max() <=      */
+/* 1024, symmetric: j in row i exactly when i is in row j); coords, u,       */
+/* force, bc_values, force_bc_values (nnodes, 3) f64; bc_types,              */
+/* force_bc_types (nnodes, 3) int32; r = coords + u.                         */
+/*   pp_cy_break_bonds: break_bonds (pyx:102-156), the result of the loop    */
+/*     over nodes in ascending order: a bond (i, j), i < j, with             */
+/*     !(|strain| < critical_strain) is swap-removed from row i and from row */
+/*     j (vacated slots keep their stale values); n_neigh updated.           */
+/*   pp_cy_bond_force: bond_force (pyx:34-99): force[i] = the sequential sum */
+/*     from 0 of -f*vol[k] over lower neighbours k (ascending), +f*vol[j]    */
+/*     over upper neighbours (row order), then force_bc_scale *              */
+/*     force_bc_values where force_bc_types != 0.                            */
+/*   pp_cy_update_displacement: update_displacement (pyx:159-184).          */
+/*   pp_cy_damage: damage (pyx:5-31), (family - n_neigh) / family.          */
+/* ------------------------------------------------------------------------ */
+
+int pp_cy_break_bonds(const double* coords, const double* u, int32_t* nlist, int32_t* n_neigh,
+                      int32_t nnodes, int32_t max_neigh, double critical_strain, void* stream);
+int pp_cy_bond_force(const double* coords, const double* u, const int32_t* nlist,
+                     const int32_t* n_neigh, const double* volume, double bond_stiffness,
+                     const double* force_bc_values, const int32_t* force_bc_types,
+                     double force_bc_scale, int32_t nnodes, int32_t max_neigh, double* force,
+                     void* stream);
+int pp_cy_update_displacement(double* u, const double* bc_values, const int32_t* bc_types,
+                              const double* force, double bc_scale, double dt, int32_t nnodes,
+                              void* stream);
+int pp_cy_damage(const int32_t* n_neigh, const int32_t* family, int32_t nnodes, double* damage,
+                 void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Write-step sums.  Replace the NumPy reductions Model.simulate runs at    */
 /* every write (peripy/model.py:1320-1366), so that a write needs to copy   */
 /* back only u and damage (the mesh file's fields).                         */

@@ -150,6 +150,13 @@ SIGNATURES = {
                                        _vp, _vp]),
     "pp_pairwise_plan": (ctypes.c_int64, [_i64, _vp, _i64]),
     "pp_bond_lengths": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
+    "pp_cy_break_bonds": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i32, _i32,
+                                         _f64, _vp]),
+    "pp_cy_bond_force": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _f64, _vp,
+                                        _vp, _f64, _i32, _i32, _vp, _vp]),
+    "pp_cy_update_displacement": (ctypes.c_int, [_vp, _vp, _vp, _vp, _f64,
+                                                 _f64, _i32, _vp]),
+    "pp_cy_damage": (ctypes.c_int, [_vp, _vp, _i32, _vp, _vp]),
     "pp_write_sums": (ctypes.c_int, [ctypes.POINTER(WriteSumsArgs), _vp]),
     "pp_mixed_pack": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),
     "pp_mixed_export": (ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _vp]),

@@ -678,6 +678,181 @@ class _CUDAIntegrator(Integrator):
         return (u, ud, udd, force, body_force, damage, nlist, n_neigh)
 
 
+class Euler(Integrator):
+    r"""PeriPy's CPU integrator ``Euler`` (``peripy/integrators.py:303-459``)
+    on the GPU.
+
+    Same arithmetic and the same sequential semantics as the Cython step it
+    replaces (``peripy/peridynamics.pyx``), bit for bit: bonds break when
+    ``|strain| >= critical_stretch`` (tension or compression) and are
+    swap-removed from both rows; each bond pair's force is applied to both
+    nodes; ``u(t + dt) = u(t) + dt f(t)``.  As in the reference, the
+    ``context`` attribute is None, so :class:`~.model.Model` builds the
+    compact, 0-padded neighbour list this step works on; the kernels run on
+    a :class:`CUDAContext` of their own (``device_context``, device 0 by
+    default).  Bond types, n-linear damage, stiffness corrections and
+    densities are rejected as the reference rejects them.
+    """
+
+    def __init__(self, dt, device_context=None):
+        """Create an :class:`Euler` integrator object.
+
+        :arg float dt: The length of time (in seconds [s]) of one time-step.
+        :arg device_context: Optional :class:`CUDAContext` for the kernels.
+        """
+        if device_context is not None and not isinstance(device_context,
+                                                         CUDAContext):
+            raise TypeError("device_context must be a CUDAContext object")
+        self.dt = dt
+        # Not a device-layout integrator: Model builds the compact layout
+        self.context = None
+        self._device = device_context
+        lib()  # fail loudly now if the CUDA library is missing
+
+    @property
+    def device_context(self):
+        if self._device is None:
+            self._device = CUDAContext(0)
+        return self._device
+
+    def _dev(self, array, dtype, shape=None):
+        import torch
+        a = np.ascontiguousarray(array, dtype=dtype)
+        if shape is not None:
+            a = a.reshape(shape)
+        return torch.as_tensor(a, device=self.device_context.device).clone()
+
+    def build(self, nnodes, degrees_freedom, max_neighbours, coords, volume,
+              family, bc_types, bc_values, force_bc_types, force_bc_values,
+              stiffness_corrections, bond_types, densities):
+        """Initiate integrator arrays (``peripy/integrators.py:371-412``)."""
+        if bond_types is not None:
+            raise ValueError("bond_types are not supported by this "
+                             "integrator (expected {}, got {}), please use "
+                             "EulerCL instead".format(type(None),
+                                                      type(bond_types)))
+        if stiffness_corrections is not None:
+            raise ValueError("stiffness_corrections are not supported by this "
+                             "integrator (expected {}, got {}), please use "
+                             "EulerCL instead".format(
+                                 type(None), type(stiffness_corrections)))
+        if densities is not None:
+            raise ValueError("densities are not supported by this "
+                             "integrator (expected {}, got {}). This "
+                             " integrator neglects inertial effects. Do not "
+                             "supply a density or is_density argument or, "
+                             "alternatively, please use a dynamic integrator, "
+                             "such as EulerCromerCL.".format(type(None),
+                                                             type(densities)))
+        n = int(nnodes)
+        self.nnodes = n
+        self.coords = coords
+        self.family = family
+        self.volume = volume
+        self.bc_types = bc_types
+        self.bc_values = bc_values
+        self.force_bc_types = force_bc_types
+        self.force_bc_values = force_bc_values
+        with self.device_context.on_stream():
+            self._coords_d = self._dev(coords, np.float64, (n, 3))
+            self._volume_d = self._dev(volume, np.float64, (n,))
+            self._family_d = self._dev(family, np.int32, (n,))
+            self._bc_types_d = self._dev(bc_types, np.int32, (n, 3))
+            self._bc_values_d = self._dev(bc_values, np.float64, (n, 3))
+            self._fc_types_d = self._dev(force_bc_types, np.int32, (n, 3))
+            self._fc_values_d = self._dev(force_bc_values, np.float64, (n, 3))
+
+    def create_buffers(self, nlist, n_neigh, bond_stiffness, critical_stretch,
+                       plus_cs, u, ud, udd, force, body_force, damage, regimes,
+                       nregimes, nbond_types):
+        """Initiate the simulation arrays (``peripy/integrators.py:351-369``).
+        """
+        if nregimes != 1:
+            raise ValueError("n-linear damage model's are not supported by "
+                             "this integrator. Please supply just one "
+                             "bond_stiffness.")
+        if nbond_types != 1:
+            raise ValueError("n-material composite models are not supported by"
+                             " this integrator. Please supply just one "
+                             "material type and bond_stiffness.")
+        import torch
+        self.nlist = nlist
+        self.n_neigh = n_neigh
+        self.bond_stiffness = bond_stiffness
+        self.critical_stretch = critical_stretch
+        self.u = u
+        self.ud = ud
+        self.udd = udd
+        self.force = force
+        self.body_force = body_force
+        n = self.nnodes
+        width = int(np.shape(nlist)[1]) if np.ndim(nlist) == 2 else 0
+        if width > 1024:
+            raise ValueError("the neighbour list is wider than 1024 (got "
+                             f"{width})")
+        self._width = width
+        with self.device_context.on_stream():
+            self._nlist_d = self._dev(nlist, np.int32, (n, width))
+            self._n_neigh_d = self._dev(n_neigh, np.int32, (n,))
+            self._u_d = self._dev(u, np.float64, (n, 3))
+            self._force_d = self._dev(force, np.float64, (n, 3))
+            self._damage_d = torch.empty(n, dtype=torch.float64,
+                                         device=self.device_context.device)
+
+    def __call__(self, displacement_bc_magnitude, force_bc_magnitude):
+        """One step: break bonds, bond forces, Euler update
+        (``peripy/integrators.py:330-349``)."""
+        ctx = self.device_context
+        st = ctx.stream_handle
+        L = lib()
+        n, w = self.nnodes, self._width
+        with ctx.on_stream():
+            check(L.pp_cy_break_bonds(
+                _ptr(self._coords_d), _ptr(self._u_d), _ptr(self._nlist_d),
+                _ptr(self._n_neigh_d), n, w, float(self.critical_stretch),
+                st), "pp_cy_break_bonds")
+            check(L.pp_cy_bond_force(
+                _ptr(self._coords_d), _ptr(self._u_d), _ptr(self._nlist_d),
+                _ptr(self._n_neigh_d), _ptr(self._volume_d),
+                float(self.bond_stiffness), _ptr(self._fc_values_d),
+                _ptr(self._fc_types_d), float(force_bc_magnitude), n, w,
+                _ptr(self._force_d), st), "pp_cy_bond_force")
+            check(L.pp_cy_update_displacement(
+                _ptr(self._u_d), _ptr(self._bc_values_d),
+                _ptr(self._bc_types_d), _ptr(self._force_d),
+                float(displacement_bc_magnitude), float(self.dt), n, st),
+                "pp_cy_update_displacement")
+
+    def write(self, damage, u, ud, udd, force, body_force, nlist, n_neigh):
+        """Return the state variable arrays (``peripy/integrators.py:
+        452-459``): the arrays given to :meth:`create_buffers`, filled from
+        the device, and a new damage array.  The arguments are ignored, as
+        the reference ignores them."""
+        ctx = self.device_context
+        put = _CUDAIntegrator._put
+        with ctx.on_stream():
+            check(lib().pp_cy_damage(_ptr(self._n_neigh_d),
+                                     _ptr(self._family_d), self.nnodes,
+                                     _ptr(self._damage_d), ctx.stream_handle),
+                  "pp_cy_damage")
+            ctx.stream.synchronize()
+            self.u = put(self.u, self._u_d)
+            self.force = put(self.force, self._force_d)
+            self.nlist = put(self.nlist, self._nlist_d)
+            self.n_neigh = put(self.n_neigh, self._n_neigh_d)
+            damage = self._damage_d.cpu().numpy()
+        return (self.u, self.ud, self.udd, self.force, self.body_force, damage,
+                self.nlist, self.n_neigh)
+
+    def _create_special_buffers(self):
+        """Create buffers that are special to the Euler integrator."""
+        # There are none
+
+    def _build_special(self):
+        """Build programs that are special to the Euler integrator."""
+        # There are none
+
+
 class EulerCUDA(_CUDAIntegrator):
     r"""Euler integrator on CUDA (replaces ``EulerCL``, integrators.py:462).
 

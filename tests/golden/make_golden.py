@@ -18,7 +18,10 @@ Outputs:
                    expected volume, the basic CL connectivity (before the
                    crack), and the expected state after 10 steps of each CL
                    integrator (Euler: u, force, damage, nlist, n_neigh;
-                   Euler-Cromer adds ud; Velocity-Verlet adds ud, udd).
+                   Euler-Cromer adds ud; Velocity-Verlet adds ud, udd);
+                   and the Cython integrator's compact connectivity before
+                   the crack and after the crack and 10 steps
+                   (``test_integrators.py:150-195``).
 ``force3.npz``     the three-node mesh of the force test.
 """
 import pathlib
@@ -39,6 +42,8 @@ def main(reference_root):
     crack = np.load(data / "expected_connectivity_crack_cl.npz")
     ec_conn = np.load(data / "expected_connectivity_euler_cromer_cl.npz")
     vv_conn = np.load(data / "expected_connectivity_velocity_verlet_cl.npz")
+    cy_basic = np.load(data / "expected_connectivity_basic.npz")
+    cy_crack = np.load(data / "expected_connectivity_crack.npz")
     out = dict(
         points=mesh.points,
         cells_triangle=mesh.cells_dict["triangle"].astype(np.int32),
@@ -60,6 +65,10 @@ def main(reference_root):
         vv_force=np.load(data / "expected_force_velocity_verlet.npy"),
         vv_damage=np.load(data / "expected_damage_velocity_verlet.npy"),
         vv_nlist=vv_conn["nlist"], vv_n_neigh=vv_conn["n_neigh"],
+        # the Cython integrator's compact layout (0-padded, width 68):
+        # before the crack, and after the crack and 10 Euler steps
+        cy_nlist_basic=cy_basic["nlist"], cy_n_neigh_basic=cy_basic["n_neigh"],
+        cy_nlist_crack=cy_crack["nlist"], cy_n_neigh_crack=cy_crack["n_neigh"],
     )
     np.savez_compressed(HERE / "plate2113.npz", **out)
     force_mesh = read_vtk(data / "force_test.vtk")

@@ -124,3 +124,19 @@ def test_reference_cython_plate(plate, golden, ref_module):
     assert np.max(np.abs(force - st.force)) / np.max(
         np.abs(st.force)) < 1e-10
     assert np.array_equal(n_neigh, golden["euler_n_neigh"])
+
+
+def test_reference_cython_layout_goldens(golden, ref_module):
+    from tests.cython_setup import cython_plate, run_reference_euler
+    """The Cython integrator's regression (test_integrators.py:150-195) on
+    its own layout: the golden connectivity after the crack and 10 steps is
+    reproduced exactly, the displacements and forces to 1e-11."""
+    setup = cython_plate(golden)
+    u, force, damage, nlist, n_neigh = run_reference_euler(
+        ref_module, setup, STEPS, DISP_MAGS, DT, BOND_STIFFNESS,
+        CRITICAL_STRETCH)
+    assert np.array_equal(nlist, golden["cy_nlist_crack"])
+    assert np.array_equal(n_neigh, golden["cy_n_neigh_crack"])
+    for got, want in ((u, golden["euler_u"]), (force, golden["euler_force"])):
+        assert np.max(np.abs(got - want)) / np.max(np.abs(want)) < 1e-11
+    assert np.allclose(damage, golden["euler_damage"])
