@@ -373,6 +373,13 @@ int pp_cy_bond_force(const double* coords, const double* u, const int32_t* nlist
                      const double* force_bc_values, const int32_t* force_bc_types,
                      double force_bc_scale, int32_t nnodes, int32_t max_neigh, double* force,
                      void* stream);
+/* break_bonds then bond_force in one pass, with the results of the two
+ * calls above (each bond's length and strain computed once). */
+int pp_cy_break_and_force(const double* coords, const double* u, int32_t* nlist,
+                          int32_t* n_neigh, const double* volume, double bond_stiffness,
+                          double critical_strain, const double* force_bc_values,
+                          const int32_t* force_bc_types, double force_bc_scale, int32_t nnodes,
+                          int32_t max_neigh, double* force, void* stream);
 int pp_cy_update_displacement(double* u, const double* bc_values, const int32_t* bc_types,
                               const double* force, double bc_scale, double dt, int32_t nnodes,
                               void* stream);

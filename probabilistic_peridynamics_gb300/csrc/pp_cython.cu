@@ -235,6 +235,164 @@ __global__ void __launch_bounds__(kWarps * 32)
     }
 }
 
+// break_bonds then bond_force in one pass, one warp per node: each entry's
+// length and strain are computed once (with the lower node first, as both
+// Cython functions compute them), the row is edited as k_cy_break edits it
+// (the values move with their entries), and the surviving entries' terms
+// are summed in k_cy_force's order.  The force of node i depends only on
+// its own row after the breaks, so no other warp is involved.
+// Shared memory per warp and slot: entry, flag, key, order (int32); length,
+// strain and three terms (double).
+template <int kWarps>
+__global__ void __launch_bounds__(kWarps * 32)
+    k_cy_break_force(const double* __restrict__ coords, const double* __restrict__ u,
+                     int32_t* __restrict__ nlist, int32_t* __restrict__ n_neigh,
+                     const double* __restrict__ vol, double k, double critical,
+                     const double* __restrict__ fc_values, const int32_t* __restrict__ fc_types,
+                     double fc_scale, int nnodes, int width, double* __restrict__ force) {
+    extern __shared__ double fsm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int i = blockIdx.x * kWarps + warp;
+    if (i >= nnodes) return;  // warp-uniform
+    double* len = fsm + (size_t)warp * 5 * width;
+    double* str = len + width;
+    double* term = str + width;
+    int32_t* ibase = reinterpret_cast<int32_t*>(fsm + (size_t)kWarps * 5 * width);
+    int32_t* row = ibase + (size_t)warp * 4 * width;
+    int32_t* flag = row + width;
+    int32_t* key = flag + width;
+    int32_t* order = key + width;
+    int32_t* g = nlist + (int64_t)i * width;
+    const int cnt0 = min(max(n_neigh[i], 0), width);
+    const V3 ri = pos(coords, u, i);
+    const V3 r0i = at(coords, i);
+    bool any = false;
+    for (int p = lane; p < cnt0; p += 32) {
+        const int j = g[p];
+        int f = 0;
+        double l = 0.0, st = 0.0;
+        if (j >= 0 && j < nnodes && j != i) {
+            const V3 rj = pos(coords, u, j);
+            const V3 r0j = at(coords, j);
+            if (j < i) {
+                l = ceuclid(rj, ri);
+                st = cstrain2(l, r0j, r0i);
+                f = kLower;
+            } else {
+                l = ceuclid(ri, rj);
+                st = cstrain2(l, r0i, r0j);
+                f = kUpper;
+            }
+            if (!(fabs(st) < critical)) f |= kBroken;
+        }
+        row[p] = j;
+        flag[p] = f;
+        len[p] = l;
+        str[p] = st;
+        any |= (f & kBroken) != 0;
+    }
+    const bool edited = __any_sync(kFull, any);
+    __syncwarp();
+    int cnt = cnt0;
+    if (edited) {
+        auto move = [&](int to, int from) {
+            row[to] = row[from];
+            flag[to] = flag[from];
+            len[to] = len[from];
+            str[to] = str[from];
+        };
+        int last = -1;
+        while (true) {
+            int best = INT32_MAX;
+            for (int p = lane; p < cnt; p += 32)
+                if ((flag[p] & (kLower | kBroken)) == (kLower | kBroken) && row[p] > last &&
+                    row[p] < best)
+                    best = row[p];
+            for (int off = 16; off > 0; off >>= 1)
+                best = min(best, __shfl_xor_sync(kFull, best, off));
+            if (best == INT32_MAX) break;
+            last = best;
+            int hit = -1;
+            for (int p0 = 0; p0 < cnt && hit < 0; p0 += 32) {
+                const int p = p0 + lane;
+                const unsigned m = __ballot_sync(kFull, p < cnt && row[p] == best);
+                if (m) hit = p0 + __ffs(m) - 1;
+            }
+            if (hit >= 0) {
+                if (lane == 0) move(hit, cnt - 1);
+                --cnt;
+            }
+            __syncwarp();
+        }
+        int next = 0;
+        while (true) {
+            int hit = -1;
+            for (int p0 = next; p0 < cnt && hit < 0; p0 += 32) {
+                const int p = p0 + lane;
+                const unsigned m = __ballot_sync(
+                    kFull, p < cnt && (flag[p] & (kUpper | kBroken)) == (kUpper | kBroken));
+                if (m) hit = p0 + __ffs(m) - 1;
+            }
+            if (hit < 0) break;
+            if (lane == 0) move(hit, cnt - 1);
+            --cnt;
+            next = hit;
+            __syncwarp();
+        }
+        __syncwarp();
+        for (int p = lane; p < cnt0; p += 32) g[p] = row[p];
+        if (lane == 0) n_neigh[i] = cnt;
+    }
+    // bond_force on the edited row
+    for (int p = lane; p < cnt; p += 32) {
+        const int f = flag[p];
+        int kk = -1;
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+        if (f & (kLower | kUpper)) {
+            const int j = row[p];
+            const V3 rj = pos(coords, u, j);
+            const double fn = ddiv(dmul(str[p], k), len[p]);
+            if (f & kLower) {
+                t0 = dmul(dmul(fn, dsub(ri.x, rj.x)), vol[j]);
+                t1 = dmul(dmul(fn, dsub(ri.y, rj.y)), vol[j]);
+                t2 = dmul(dmul(fn, dsub(ri.z, rj.z)), vol[j]);
+                kk = j;
+            } else {
+                t0 = dmul(dmul(fn, dsub(rj.x, ri.x)), vol[j]);
+                t1 = dmul(dmul(fn, dsub(rj.y, ri.y)), vol[j]);
+                t2 = dmul(dmul(fn, dsub(rj.z, ri.z)), vol[j]);
+                kk = nnodes + p;
+            }
+        }
+        term[3 * p] = t0;
+        term[3 * p + 1] = t1;
+        term[3 * p + 2] = t2;
+        key[p] = kk;
+    }
+    __syncwarp();
+    int used = 0;
+    for (int p = 0; p < cnt; ++p) used += key[p] >= 0;
+    for (int p = lane; p < cnt; p += 32) {
+        const int kp = key[p];
+        if (kp < 0) continue;
+        int rank = 0;
+        for (int q = 0; q < cnt; ++q) rank += key[q] >= 0 && key[q] < kp;
+        order[rank] = p;
+    }
+    __syncwarp();
+    if (lane < 3) {
+        double acc = 0.0;
+        for (int r = 0; r < used; ++r) {
+            const int p = order[r];
+            const double t = term[3 * p + lane];
+            acc = key[p] < nnodes ? dsub(acc, t) : dadd(acc, t);
+        }
+        const int64_t o = 3 * (int64_t)i + lane;
+        if (fc_types[o] != 0) acc = dadd(acc, dmul(fc_scale, fc_values[o]));
+        force[o] = acc;
+    }
+}
+
 // update_displacement (peridynamics.pyx:159-184)
 __global__ void k_cy_update(double* __restrict__ u, const double* __restrict__ bc_values,
                             const int32_t* __restrict__ bc_types,
@@ -328,6 +486,56 @@ extern "C" int pp_cy_bond_force(const double* coords, const double* u, const int
             return launch_force<1>(coords, u, nlist, n_neigh, volume, bond_stiffness,
                                    force_bc_values, force_bc_types, force_bc_scale, nnodes,
                                    max_neigh, force, st);
+    }
+}
+
+namespace {
+
+template <int W>
+int launch_break_force(const double* coords, const double* u, int32_t* nlist, int32_t* n_neigh,
+                       const double* vol, double k, double critical, const double* fcv,
+                       const int32_t* fct, double scale, int n, int width, double* force,
+                       cudaStream_t st) {
+    const size_t smem = (size_t)W * width * (5 * sizeof(double) + 4 * sizeof(int32_t));
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_cy_break_force<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+        return PP_ERROR_CUDA;
+    k_cy_break_force<W><<<(n + W - 1) / W, W * 32, smem, st>>>(
+        coords, u, nlist, n_neigh, vol, k, critical, fcv, fct, scale, n, width, force);
+    return launch_status();
+}
+
+}  // namespace
+
+extern "C" int pp_cy_break_and_force(const double* coords, const double* u, int32_t* nlist,
+                                     int32_t* n_neigh, const double* volume,
+                                     double bond_stiffness, double critical_strain,
+                                     const double* force_bc_values,
+                                     const int32_t* force_bc_types, double force_bc_scale,
+                                     int32_t nnodes, int32_t max_neigh, double* force,
+                                     void* stream) {
+    if (nnodes < 0 || max_neigh < 0) return PP_ERROR_INVALID_VALUE;
+    if (max_neigh > kMaxWidth) return PP_ERROR_MAX_NEIGH;
+    if (nnodes == 0) return PP_SUCCESS;
+    if (!coords || !u || (max_neigh > 0 && !nlist) || !n_neigh || !volume || !force_bc_values ||
+        !force_bc_types || !force)
+        return PP_ERROR_INVALID_VALUE;
+    const int width = max_neigh > 0 ? max_neigh : 1;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (warps_for((size_t)width * (5 * sizeof(double) + 4 * sizeof(int32_t)))) {
+        case 4:
+            return launch_break_force<4>(coords, u, nlist, n_neigh, volume, bond_stiffness,
+                                         critical_strain, force_bc_values, force_bc_types,
+                                         force_bc_scale, nnodes, max_neigh, force, st);
+        case 2:
+            return launch_break_force<2>(coords, u, nlist, n_neigh, volume, bond_stiffness,
+                                         critical_strain, force_bc_values, force_bc_types,
+                                         force_bc_scale, nnodes, max_neigh, force, st);
+        default:
+            return launch_break_force<1>(coords, u, nlist, n_neigh, volume, bond_stiffness,
+                                         critical_strain, force_bc_values, force_bc_types,
+                                         force_bc_scale, nnodes, max_neigh, force, st);
     }
 }
 

@@ -694,16 +694,20 @@ class Euler(Integrator):
     densities are rejected as the reference rejects them.
     """
 
-    def __init__(self, dt, device_context=None):
+    def __init__(self, dt, device_context=None, fused=True):
         """Create an :class:`Euler` integrator object.
 
         :arg float dt: The length of time (in seconds [s]) of one time-step.
         :arg device_context: Optional :class:`CUDAContext` for the kernels.
+        :arg bool fused: True: bond breaking and bond forces in one kernel
+            (``pp_cy_break_and_force``, each bond's strain computed once);
+            False: one kernel per Cython function.  Same results.
         """
         if device_context is not None and not isinstance(device_context,
                                                          CUDAContext):
             raise TypeError("device_context must be a CUDAContext object")
         self.dt = dt
+        self.fused = bool(fused)
         # Not a device-layout integrator: Model builds the compact layout
         self.context = None
         self._device = device_context
@@ -807,21 +811,34 @@ class Euler(Integrator):
         L = lib()
         n, w = self.nnodes, self._width
         with ctx.on_stream():
-            check(L.pp_cy_break_bonds(
-                _ptr(self._coords_d), _ptr(self._u_d), _ptr(self._nlist_d),
-                _ptr(self._n_neigh_d), n, w, float(self.critical_stretch),
-                st), "pp_cy_break_bonds")
-            check(L.pp_cy_bond_force(
-                _ptr(self._coords_d), _ptr(self._u_d), _ptr(self._nlist_d),
-                _ptr(self._n_neigh_d), _ptr(self._volume_d),
-                float(self.bond_stiffness), _ptr(self._fc_values_d),
-                _ptr(self._fc_types_d), float(force_bc_magnitude), n, w,
-                _ptr(self._force_d), st), "pp_cy_bond_force")
+            if self.fused:
+                check(L.pp_cy_break_and_force(
+                    _ptr(self._coords_d), _ptr(self._u_d),
+                    _ptr(self._nlist_d), _ptr(self._n_neigh_d),
+                    _ptr(self._volume_d), float(self.bond_stiffness),
+                    float(self.critical_stretch), _ptr(self._fc_values_d),
+                    _ptr(self._fc_types_d), float(force_bc_magnitude), n, w,
+                    _ptr(self._force_d), st), "pp_cy_break_and_force")
+            else:
+                self._break_and_force(L, n, w, force_bc_magnitude, st)
             check(L.pp_cy_update_displacement(
                 _ptr(self._u_d), _ptr(self._bc_values_d),
                 _ptr(self._bc_types_d), _ptr(self._force_d),
                 float(displacement_bc_magnitude), float(self.dt), n, st),
                 "pp_cy_update_displacement")
+
+    def _break_and_force(self, L, n, w, force_bc_magnitude, st):
+        """break_bonds and bond_force as two kernels."""
+        check(L.pp_cy_break_bonds(
+            _ptr(self._coords_d), _ptr(self._u_d), _ptr(self._nlist_d),
+            _ptr(self._n_neigh_d), n, w, float(self.critical_stretch), st),
+            "pp_cy_break_bonds")
+        check(L.pp_cy_bond_force(
+            _ptr(self._coords_d), _ptr(self._u_d), _ptr(self._nlist_d),
+            _ptr(self._n_neigh_d), _ptr(self._volume_d),
+            float(self.bond_stiffness), _ptr(self._fc_values_d),
+            _ptr(self._fc_types_d), float(force_bc_magnitude), n, w,
+            _ptr(self._force_d), st), "pp_cy_bond_force")
 
     def write(self, damage, u, ud, udd, force, body_force, nlist, n_neigh):
         """Return the state variable arrays (``peripy/integrators.py:

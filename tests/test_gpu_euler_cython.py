@@ -30,10 +30,10 @@ def ref():
     return build_ref.load()
 
 
-def run_gpu_euler(setup, steps, mags, dt, k, s0, fmags=None):
+def run_gpu_euler(setup, steps, mags, dt, k, s0, fmags=None, fused=True):
     import probabilistic_peridynamics_gb300 as pp
     n = setup["coords"].shape[0]
-    integ = pp.Euler(dt)
+    integ = pp.Euler(dt, fused=fused)
     assert integ.context is None
     integ.build(n, 3, setup["nlist"].shape[1], setup["coords"],
                 setup["volume"], setup["family"], setup["bc_types"],
@@ -56,12 +56,13 @@ def _same(got, want):
         assert np.array_equal(g, w, equal_nan=True)
 
 
-def test_regression_plate(golden, ref):
+@pytest.mark.parametrize("fused", [True, False])
+def test_regression_plate(golden, ref, fused):
     """test_integrators.py:150-195 on the GPU: 10 steps of the cracked
     plate in the Cython layout."""
     setup = cython_plate(golden)
     got = run_gpu_euler(setup, STEPS, DISP_MAGS, DT, BOND_STIFFNESS,
-                        CRITICAL_STRETCH)
+                        CRITICAL_STRETCH, fused=fused)
     _same(got, run_reference_euler(ref, setup, STEPS, DISP_MAGS, DT,
                                    BOND_STIFFNESS, CRITICAL_STRETCH))
     assert np.array_equal(got[3], golden["cy_nlist_crack"])
@@ -99,7 +100,8 @@ def _breaking_lattice():
                 force_bc_values=fcv)
 
 
-def test_breaking_lattice_with_force_boundaries(ref):
+@pytest.mark.parametrize("fused", [True, False])
+def test_breaking_lattice_with_force_boundaries(ref, fused):
     """Bonds break in tension (pulled faces) and in compression (the
     loaded top face) and are swap-removed from both rows, many per row."""
     setup = _breaking_lattice()
@@ -107,7 +109,7 @@ def test_breaking_lattice_with_force_boundaries(ref):
     mags = 2e-3 * np.arange(1, steps + 1)
     fmags = 0.05 * np.arange(1, steps + 1)
     args = (setup, steps, mags, 0.5, 0.05, 0.01)
-    got = run_gpu_euler(*args, fmags=fmags)
+    got = run_gpu_euler(*args, fmags=fmags, fused=fused)
     want = run_reference_euler(ref, *args, fmags=fmags)
     _same(got, want)
     broken = int(setup["family"].sum() - want[4].sum())
