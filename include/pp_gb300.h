@@ -281,7 +281,8 @@ int pp_bond_extent(const int32_t* nlist, const double* r0, int32_t nnodes,
  * length[i * max_neigh + k] = sqrt((x*x + y*y) + z*z) in binary64 with
  * (x, y, z) = r0[j] - r0[i], j = nlist[i * max_neigh + k], the value the
  * step computes for xi (peripy/cl/peridynamics.cl:65-73); 0 where j is -1.
- * A length stays valid while nlist only loses bonds (set to -1). */
+ * A length stays valid while nlist only loses bonds (set to -1).
+ * max_neigh: 1..1024 (any width: the compact rows of pp_cy_* too). */
 int pp_bond_lengths(const double* r0, const int32_t* nlist, int32_t nnodes,
                     int32_t max_neigh, double* length, void* stream);
 
@@ -374,12 +375,15 @@ int pp_cy_bond_force(const double* coords, const double* u, const int32_t* nlist
                      double force_bc_scale, int32_t nnodes, int32_t max_neigh, double* force,
                      void* stream);
 /* break_bonds then bond_force in one pass, with the results of the two
- * calls above (each bond's length and strain computed once). */
+ * calls above (each bond's length and strain computed once).  bond_length
+ * (optional, (nnodes, max_neigh) f64, in/out): the reference length of
+ * each entry, as pp_bond_lengths writes it; read instead of computed, and
+ * kept in the order of the entries as rows are edited.  NULL: computed. */
 int pp_cy_break_and_force(const double* coords, const double* u, int32_t* nlist,
                           int32_t* n_neigh, const double* volume, double bond_stiffness,
                           double critical_strain, const double* force_bc_values,
                           const int32_t* force_bc_types, double force_bc_scale, int32_t nnodes,
-                          int32_t max_neigh, double* force, void* stream);
+                          int32_t max_neigh, double* force, double* bond_length, void* stream);
 int pp_cy_update_displacement(double* u, const double* bc_values, const int32_t* bc_types,
                               const double* force, double bc_scale, double dt, int32_t nnodes,
                               void* stream);

@@ -156,7 +156,7 @@ SIGNATURES = {
                                         _vp, _f64, _i32, _i32, _vp, _vp]),
     "pp_cy_break_and_force": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _f64,
                                              _f64, _vp, _vp, _f64, _i32,
-                                             _i32, _vp, _vp]),
+                                             _i32, _vp, _vp, _vp]),
     "pp_cy_update_displacement": (ctypes.c_int, [_vp, _vp, _vp, _vp, _f64,
                                                  _f64, _i32, _vp]),
     "pp_cy_damage": (ctypes.c_int, [_vp, _vp, _i32, _vp, _vp]),

@@ -241,23 +241,28 @@ __global__ void __launch_bounds__(kWarps * 32)
 // (the values move with their entries), and the surviving entries' terms
 // are summed in k_cy_force's order.  The force of node i depends only on
 // its own row after the breaks, so no other warp is involved.
-// Shared memory per warp and slot: entry, flag, key, order (int32); length,
-// strain and three terms (double).
+// With l0c (the per-slot reference lengths, (nnodes, width), kept in the
+// order of the row's entries) the reference length is read instead of
+// computed, and moves with its entry.  Shared memory per warp and slot:
+// entry, flag, key, order (int32); length, strain, reference length and
+// three terms (double).
 template <int kWarps>
 __global__ void __launch_bounds__(kWarps * 32)
     k_cy_break_force(const double* __restrict__ coords, const double* __restrict__ u,
                      int32_t* __restrict__ nlist, int32_t* __restrict__ n_neigh,
                      const double* __restrict__ vol, double k, double critical,
                      const double* __restrict__ fc_values, const int32_t* __restrict__ fc_types,
-                     double fc_scale, int nnodes, int width, double* __restrict__ force) {
+                     double fc_scale, int nnodes, int width, double* __restrict__ force,
+                     double* __restrict__ l0c) {
     extern __shared__ double fsm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int i = blockIdx.x * kWarps + warp;
     if (i >= nnodes) return;  // warp-uniform
-    double* len = fsm + (size_t)warp * 5 * width;
+    double* len = fsm + (size_t)warp * 6 * width;
     double* str = len + width;
-    double* term = str + width;
-    int32_t* ibase = reinterpret_cast<int32_t*>(fsm + (size_t)kWarps * 5 * width);
+    double* ref = str + width;
+    double* term = ref + width;
+    int32_t* ibase = reinterpret_cast<int32_t*>(fsm + (size_t)kWarps * 6 * width);
     int32_t* row = ibase + (size_t)warp * 4 * width;
     int32_t* flag = row + width;
     int32_t* key = flag + width;
@@ -266,29 +271,34 @@ __global__ void __launch_bounds__(kWarps * 32)
     const int cnt0 = min(max(n_neigh[i], 0), width);
     const V3 ri = pos(coords, u, i);
     const V3 r0i = at(coords, i);
+    double* gl0 = l0c ? l0c + (int64_t)i * width : nullptr;
     bool any = false;
     for (int p = lane; p < cnt0; p += 32) {
         const int j = g[p];
         int f = 0;
-        double l = 0.0, st = 0.0;
+        double l = 0.0, st = 0.0, l0 = gl0 ? gl0[p] : 0.0;
         if (j >= 0 && j < nnodes && j != i) {
             const V3 rj = pos(coords, u, j);
             const V3 r0j = at(coords, j);
+            // cstrain2 with the lower node first; the cached l0 is the
+            // same value (ceuclid of the two reference positions)
             if (j < i) {
                 l = ceuclid(rj, ri);
-                st = cstrain2(l, r0j, r0i);
+                if (!gl0) l0 = ceuclid(r0j, r0i);
                 f = kLower;
             } else {
                 l = ceuclid(ri, rj);
-                st = cstrain2(l, r0i, r0j);
+                if (!gl0) l0 = ceuclid(r0i, r0j);
                 f = kUpper;
             }
+            st = ddiv(dsub(l, l0), l0);
             if (!(fabs(st) < critical)) f |= kBroken;
         }
         row[p] = j;
         flag[p] = f;
         len[p] = l;
         str[p] = st;
+        ref[p] = l0;
         any |= (f & kBroken) != 0;
     }
     const bool edited = __any_sync(kFull, any);
@@ -300,6 +310,7 @@ __global__ void __launch_bounds__(kWarps * 32)
             flag[to] = flag[from];
             len[to] = len[from];
             str[to] = str[from];
+            ref[to] = ref[from];
         };
         int last = -1;
         while (true) {
@@ -340,7 +351,10 @@ __global__ void __launch_bounds__(kWarps * 32)
             __syncwarp();
         }
         __syncwarp();
-        for (int p = lane; p < cnt0; p += 32) g[p] = row[p];
+        for (int p = lane; p < cnt0; p += 32) {
+            g[p] = row[p];
+            if (gl0) gl0[p] = ref[p];
+        }
         if (lane == 0) n_neigh[i] = cnt;
     }
     // bond_force on the edited row
@@ -495,14 +509,14 @@ template <int W>
 int launch_break_force(const double* coords, const double* u, int32_t* nlist, int32_t* n_neigh,
                        const double* vol, double k, double critical, const double* fcv,
                        const int32_t* fct, double scale, int n, int width, double* force,
-                       cudaStream_t st) {
-    const size_t smem = (size_t)W * width * (5 * sizeof(double) + 4 * sizeof(int32_t));
+                       double* l0c, cudaStream_t st) {
+    const size_t smem = (size_t)W * width * (6 * sizeof(double) + 4 * sizeof(int32_t));
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(k_cy_break_force<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
         return PP_ERROR_CUDA;
     k_cy_break_force<W><<<(n + W - 1) / W, W * 32, smem, st>>>(
-        coords, u, nlist, n_neigh, vol, k, critical, fcv, fct, scale, n, width, force);
+        coords, u, nlist, n_neigh, vol, k, critical, fcv, fct, scale, n, width, force, l0c);
     return launch_status();
 }
 
@@ -514,7 +528,7 @@ extern "C" int pp_cy_break_and_force(const double* coords, const double* u, int3
                                      const double* force_bc_values,
                                      const int32_t* force_bc_types, double force_bc_scale,
                                      int32_t nnodes, int32_t max_neigh, double* force,
-                                     void* stream) {
+                                     double* bond_length, void* stream) {
     if (nnodes < 0 || max_neigh < 0) return PP_ERROR_INVALID_VALUE;
     if (max_neigh > kMaxWidth) return PP_ERROR_MAX_NEIGH;
     if (nnodes == 0) return PP_SUCCESS;
@@ -523,19 +537,22 @@ extern "C" int pp_cy_break_and_force(const double* coords, const double* u, int3
         return PP_ERROR_INVALID_VALUE;
     const int width = max_neigh > 0 ? max_neigh : 1;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    switch (warps_for((size_t)width * (5 * sizeof(double) + 4 * sizeof(int32_t)))) {
+    switch (warps_for((size_t)width * (6 * sizeof(double) + 4 * sizeof(int32_t)))) {
         case 4:
             return launch_break_force<4>(coords, u, nlist, n_neigh, volume, bond_stiffness,
                                          critical_strain, force_bc_values, force_bc_types,
-                                         force_bc_scale, nnodes, max_neigh, force, st);
+                                         force_bc_scale, nnodes, max_neigh, force, bond_length,
+                                         st);
         case 2:
             return launch_break_force<2>(coords, u, nlist, n_neigh, volume, bond_stiffness,
                                          critical_strain, force_bc_values, force_bc_types,
-                                         force_bc_scale, nnodes, max_neigh, force, st);
+                                         force_bc_scale, nnodes, max_neigh, force, bond_length,
+                                         st);
         default:
             return launch_break_force<1>(coords, u, nlist, n_neigh, volume, bond_stiffness,
                                          critical_strain, force_bc_values, force_bc_types,
-                                         force_bc_scale, nnodes, max_neigh, force, st);
+                                         force_bc_scale, nnodes, max_neigh, force, bond_length,
+                                         st);
     }
 }
 

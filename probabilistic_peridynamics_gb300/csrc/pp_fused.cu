@@ -267,7 +267,7 @@ extern "C" int pp_fused_run(const pp_fused_args* args, int32_t parity, int64_t n
 extern "C" int pp_bond_lengths(const double* r0, const int32_t* nlist, int32_t nnodes,
                                int32_t max_neigh, double* length, void* stream) {
     if (nnodes < 0) return PP_ERROR_INVALID_VALUE;
-    if (!is_pow2_le_1024(max_neigh)) return PP_ERROR_MAX_NEIGH;
+    if (max_neigh < 1 || max_neigh > 1024) return PP_ERROR_MAX_NEIGH;
     if (nnodes == 0) return PP_SUCCESS;
     if (!r0 || !nlist || !length) return PP_ERROR_INVALID_VALUE;
     const int64_t slots = (int64_t)nnodes * max_neigh;

@@ -700,8 +700,9 @@ class Euler(Integrator):
         :arg float dt: The length of time (in seconds [s]) of one time-step.
         :arg device_context: Optional :class:`CUDAContext` for the kernels.
         :arg bool fused: True: bond breaking and bond forces in one kernel
-            (``pp_cy_break_and_force``, each bond's strain computed once);
-            False: one kernel per Cython function.  Same results.
+            (``pp_cy_break_and_force``, each bond's strain computed once,
+            reference lengths cached per entry); False: one kernel per
+            Cython function.  Same results.
         """
         if device_context is not None and not isinstance(device_context,
                                                          CUDAContext):
@@ -802,6 +803,16 @@ class Euler(Integrator):
             self._force_d = self._dev(force, np.float64, (n, 3))
             self._damage_d = torch.empty(n, dtype=torch.float64,
                                          device=self.device_context.device)
+            self._l0_d = None
+            if self.fused and width > 0 and n > 0:
+                # reference length of every entry (the same value the step
+                # would compute), kept in entry order by the fused kernel
+                self._l0_d = torch.empty((n, width), dtype=torch.float64,
+                                         device=self.device_context.device)
+                check(lib().pp_bond_lengths(
+                    _ptr(self._coords_d), _ptr(self._nlist_d), n, width,
+                    _ptr(self._l0_d), self.device_context.stream_handle),
+                    "pp_bond_lengths")
 
     def __call__(self, displacement_bc_magnitude, force_bc_magnitude):
         """One step: break bonds, bond forces, Euler update
@@ -818,7 +829,8 @@ class Euler(Integrator):
                     _ptr(self._volume_d), float(self.bond_stiffness),
                     float(self.critical_stretch), _ptr(self._fc_values_d),
                     _ptr(self._fc_types_d), float(force_bc_magnitude), n, w,
-                    _ptr(self._force_d), st), "pp_cy_break_and_force")
+                    _ptr(self._force_d), _ptr(self._l0_d), st),
+                    "pp_cy_break_and_force")
             else:
                 self._break_and_force(L, n, w, force_bc_magnitude, st)
             check(L.pp_cy_update_displacement(

@@ -123,7 +123,9 @@ def test_validation_without_gpu(L):
 
 def test_bond_lengths_validation_without_gpu(L):
     from probabilistic_peridynamics_gb300 import _lib
-    assert L.pp_bond_lengths(None, None, 10, 3, None, None) == \
+    assert L.pp_bond_lengths(None, None, 10, 2000, None, None) == \
+        _lib.PP_ERROR_MAX_NEIGH
+    assert L.pp_bond_lengths(None, None, 10, 0, None, None) == \
         _lib.PP_ERROR_MAX_NEIGH
     assert L.pp_bond_lengths(None, None, 0, 4, None, None) == _lib.PP_SUCCESS
     assert L.pp_bond_lengths(None, None, 10, 4, None, None) == \

@@ -60,10 +60,11 @@ def test_entry_point_validation_without_gpu():
     assert L.pp_cy_bond_force(None, None, None, None, None, 1.0, None, None,
                               0.0, 5, 4, None, None) == inv
     assert L.pp_cy_break_and_force(None, None, None, None, None, 1.0, 0.1,
-                                   None, None, 0.0, 5, 2000, None,
+                                   None, None, 0.0, 5, 2000, None, None,
                                    None) == wide
     assert L.pp_cy_break_and_force(None, None, None, None, None, 1.0, 0.1,
-                                   None, None, 0.0, 5, 4, None, None) == inv
+                                   None, None, 0.0, 5, 4, None, None,
+                                   None) == inv
     assert L.pp_cy_update_displacement(None, None, None, None, 0.0, 1.0, -1,
                                        None) == inv
     assert L.pp_cy_damage(None, None, 3, None, None) == inv
