@@ -801,7 +801,10 @@ __global__ void __launch_bounds__(W * 32, MINB)
         // kNPW consecutive nodes per warp, kLPN lanes each
         constexpr int kLPN = kLanesPerNode;
         constexpr int kNPW = 32 / kLPN;
-        constexpr int kG = 4;
+        // slots per batch: 4; 2 with bond types, whose regime state and
+        // tables would otherwise hold enough registers per slot to cost a
+        // resident CTA (composite: 0.334 vs 0.367 ms per step)
+        constexpr int kG = TYPES ? 2 : 4;
         const int grp = lane / kLPN, sub = lane % kLPN;
         auto first_batch = [&](int i, int (&jn)[kG]) {
 #pragma unroll
