@@ -481,11 +481,11 @@ def compact(nlist, family):
 CPU_DT = 1e-15
 
 
-def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None, ny=NY):
-    """Time the reference CPU step on an nx x ny x 10 block of the lattice.
+def cpu_block(nx, ny=NY):
+    """The reference CPU step on an nx x ny x 10 block of the lattice.
 
-    :returns: (bond-updates/s, steps run, seconds, bonds per step, kind,
-        cores, bonds broken during the sample)
+    :returns: (step(s) function, bonds per step, kind, cores, intact()
+        function)
     """
     from probabilistic_peridynamics_gb300 import lattice
     coords = lattice.lattice_coords(nx, ny, NZ, DX)
@@ -528,6 +528,16 @@ def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None, ny=NY):
         def intact():
             return int((st.nlist != -1).sum())
         kind, cores = "port", os.cpu_count() or 1
+    return step, bonds, kind, cores, intact
+
+
+def cpu_sample(nx, budget_s, min_steps=1, max_steps=5, steps=None, ny=NY):
+    """Time the reference CPU step on an nx x ny x 10 block of the lattice.
+
+    :returns: (bond-updates/s, steps run, seconds, bonds per step, kind,
+        cores, bonds broken during the sample)
+    """
+    step, bonds, kind, cores, intact = cpu_block(nx, ny)
     t0 = time.perf_counter()
     done = 0
     while True:
@@ -573,34 +583,80 @@ def cpu_baseline():
                       f"dt {CPU_DT:g}, {broken} bonds broken), {el:.1f} s"}
 
 
+def _reference_worker(nx, ny, warmup, steps, barrier, out):
+    """One instance of the reference CPU step (a spawned process): its own
+    block, the warm-up steps, then the timed steps started together with
+    the other instances."""
+    step, bonds, kind, cores, intact = cpu_block(nx, ny)
+    for s in range(warmup):
+        step(s + 1)
+    barrier.wait()
+    t0 = time.time()
+    for s in range(steps):
+        step(warmup + s + 1)
+    t1 = time.time()
+    out.put((bonds, steps, t0, t1, kind, cores,
+             bonds - intact()))
+
+
 def reference_arm(args):
+    """The reference's own CPU step on the host cores.  The step is serial
+    (no threads in the reference), so every core available to this process
+    runs one instance of it on its own copy of the same block of the
+    lattice, all timed over the same window: the rate is the bond-updates
+    of all instances over that window."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    import multiprocessing as mp
     total = args.steps + args.warmup
+    try:
+        workers = len(os.sched_getaffinity(0))
+    except AttributeError:
+        workers = os.cpu_count() or 1
+    if reference_step_fn() is None:
+        workers = 1  # the C port threads itself (OpenMP)
     # Size the block (4 x ny x 10 of the lattice) so that warm-up + timed
-    # steps take about 90 s on one core.
+    # steps take about 90 s on one core; at most 50 x 200 x 10 per instance
+    # (each instance holds its own block).
     probe_rate, *_ = cpu_sample(4, budget_s=0.5, min_steps=1, max_steps=3)
     per_step_bonds = probe_rate * 90.0 / max(total, 1)
     bonds_4xNY = 4 * NY * NZ * 107.0  # about 107 bonds per node in bulk
     nx, ny = 4, int(max(4, min(NY, NY * per_step_bonds / bonds_4xNY)))
     if per_step_bonds > bonds_4xNY:
-        nx = int(max(4, min(NX, 4 * per_step_bonds / bonds_4xNY)))
+        nx = int(max(4, min(50, 4 * per_step_bonds / bonds_4xNY)))
         ny = NY
-    if args.warmup:
-        cpu_sample(nx, 0.0, steps=args.warmup, ny=ny)
-    rate, steps, el, bonds, kind, cores, broken = cpu_sample(
-        nx, 0.0, steps=args.steps, ny=ny)
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(workers)
+    out = ctx.Queue()
+    procs = [ctx.Process(target=_reference_worker,
+                         args=(nx, ny, args.warmup, args.steps, barrier, out))
+             for _ in range(workers)]
+    for p in procs:
+        p.start()
+    res = [out.get() for _ in procs]
+    for p in procs:
+        p.join()
+    bonds = res[0][0]
+    steps = args.steps
+    t0 = min(r[2] for r in res)
+    t1 = max(r[3] for r in res)
+    el = t1 - t0
+    rate = sum(r[0] * r[1] for r in res) / el
+    kind = res[0][4]
+    broken = res[0][6]
     what = ("the reference CPU step (Cython break_bonds + bond_force + "
             "update_displacement)" if kind == "reference" else
             "C restatement of the OpenCL step")
-    sample = (f"each step: {what} on a {nx}x{ny}x{NZ} block of the lattice "
-              f"({bonds} bonds, Euler dt {CPU_DT:g}, {broken} bonds broken "
-              f"over the run)")
+    sample = (f"each step: {what}, {workers} instances at once (one per "
+              f"core: the reference step is serial), each on a {nx}x{ny}x"
+              f"{NZ} block of the lattice ({bonds} bonds, Euler dt "
+              f"{CPU_DT:g}, {broken} bonds broken over the run)")
+    cores = workers
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+        "ms_per_step": 1e3 * el / max(steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "sample": sample,
