@@ -8,7 +8,10 @@
   bonds break.  The plain and fused FP64 steps still reproduce the oracle
   bit for bit through the blow-up (NaN where the oracle has NaN).  A stable
   labelled variant (dt = 1e-13, dt lambda_max ~ 0.3) is held to the usual
-  bars: FP64 bit-identical, mixed within 1e-5 with the same mask.
+  bars: FP64 bit-identical, mixed within 1e-5 with the same mask.  The
+  same workload through PeriPy's CPU integrator (``Euler``, on the GPU) is
+  bit-identical to the reference's compiled Cython step, as stated and
+  stable.
 * 200x200x10 pre-cracked lattice (400,000 nodes, 42.7M bonds),
   Velocity-Verlet: at this size the oracle is too slow, so the FP64 fused
   step is checked against the plain FP64 step (each pinned to the oracle at
@@ -95,6 +98,36 @@ def test_small_lattice_stable_variant(mode):
     else:
         for got, want in zip(out, ref):
             assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("dt", [1e-6, 1e-13], ids=["as_stated", "stable"])
+def test_small_lattice_cpu_integrator(dt):
+    """The plain method's own CPU integrator (``Euler``, the Cython step)
+    on the small lattice, 1000 steps, through the GPU ``Euler``: bit for
+    bit the reference's compiled ``peridynamics.pyx`` on the same compact
+    rows, through the blow-up of the stated dt as well."""
+    from oracle import build_ref
+    from probabilistic_peridynamics_gb300 import lattice
+    from tests.cython_setup import run_reference_euler
+    from tests.test_gpu_euler_cython import run_gpu_euler
+    if not build_ref.build(quiet=True):
+        pytest.skip("the compiled reference is not available")
+    ref = build_ref.load()
+    setup = _small(dt)
+    family, nlist, _ = lattice.lattice_family(20, 20, 5, 3.015, pow2=False)
+    nlist = np.where(nlist == -1, 0, nlist).astype(np.intc)  # 0-padded
+    setup = dict(setup, family=family, nlist=nlist, n_neigh=family.copy())
+    args = (setup, STEPS, MAGS, dt, setup["k"], setup["s0"])
+    with np.errstate(all="ignore"):
+        want = run_reference_euler(ref, *args)
+    got = run_gpu_euler(*args)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w, equal_nan=True)
+    broken = int(family.sum() - want[4].sum())
+    if dt == 1e-6:
+        assert broken > 1000  # the unstable step breaks bonds (|strain|)
+    else:
+        assert broken == 0 and np.all(np.isfinite(want[0]))
 
 
 @pytest.fixture(scope="module")
