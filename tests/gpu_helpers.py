@@ -95,3 +95,19 @@ def run_oracle(kind, setup, steps, disp_mags, force_mags=None, damping=0.0,
 def rel_err(a, b):
     den = np.max(np.abs(b))
     return float(np.max(np.abs(a - b)) / (den if den > 0 else 1.0))
+
+
+def breaking_setup(kind, nx=10, ny=8, nz=4):
+    """A lattice whose pulled faces break bonds within tens of steps
+    (k 0.01, s0 0.02; densities 50 for the dynamic integrators)."""
+    coords, volume, horizon, family, nlist, n_neigh = lattice(nx, ny, nz,
+                                                              1.0)
+    bc_types, bc_values = pull_bcs(coords, 0)
+    n = coords.shape[0]
+    return dict(coords=coords, volume=volume, family=family, nlist=nlist,
+                n_neigh=n_neigh, bc_types=bc_types, bc_values=bc_values,
+                force_bc_types=np.zeros((n, 3), dtype=np.intc),
+                force_bc_values=np.zeros((n, 3)),
+                densities=None if kind == "euler" else np.full((n, 3), 50.0),
+                nnodes=n, max_neigh=nlist.shape[1], k=0.01, s0=0.02,
+                dt=0.5 if kind == "euler" else 1.0)

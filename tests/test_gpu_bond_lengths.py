@@ -54,8 +54,8 @@ def test_lengths_match_numpy():
 def test_fused_step_with_and_without_cache(kind):
     import probabilistic_peridynamics_gb300 as pp
     from tests.gpu_helpers import run_integrator
-    from tests.test_gpu_parity import _breaking_setup
-    setup = _breaking_setup(kind)
+    from tests.gpu_helpers import breaking_setup
+    setup = breaking_setup(kind)
     cls = {"euler": pp.EulerCUDA, "euler_cromer": pp.EulerCromerCUDA,
            "velocity_verlet": pp.VelocityVerletCUDA}[kind]
     steps = 60

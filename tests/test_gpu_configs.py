@@ -108,8 +108,7 @@ def test_small_lattice_cpu_integrator(dt):
     rows, through the blow-up of the stated dt as well."""
     from oracle import build_ref
     from probabilistic_peridynamics_gb300 import lattice
-    from tests.cython_setup import run_reference_euler
-    from tests.test_gpu_euler_cython import run_gpu_euler
+    from tests.cython_setup import run_gpu_euler, run_reference_euler
     if not build_ref.build(quiet=True):
         pytest.skip("the compiled reference is not available")
     ref = build_ref.load()

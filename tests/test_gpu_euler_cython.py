@@ -13,7 +13,8 @@ import numpy as np
 import pytest
 
 from tests.conftest import cuda_available
-from tests.cython_setup import cython_plate, run_reference_euler
+from tests.cython_setup import (breaking_lattice, cython_plate,
+                                 run_gpu_euler, run_reference_euler)
 from tests.plate_setup import (BOND_STIFFNESS, CRITICAL_STRETCH, DISP_MAGS,
                                DT, STEPS)
 
@@ -28,27 +29,6 @@ def ref():
     if not build_ref.build(quiet=True):
         pytest.skip("the compiled reference is not available")
     return build_ref.load()
-
-
-def run_gpu_euler(setup, steps, mags, dt, k, s0, fmags=None, fused=True):
-    import probabilistic_peridynamics_gb300 as pp
-    n = setup["coords"].shape[0]
-    integ = pp.Euler(dt, fused=fused)
-    assert integ.context is None
-    integ.build(n, 3, setup["nlist"].shape[1], setup["coords"],
-                setup["volume"], setup["family"], setup["bc_types"],
-                setup["bc_values"], setup["force_bc_types"],
-                setup["force_bc_values"], None, None, None)
-    z = lambda: np.zeros((n, 3))  # noqa: E731
-    integ.create_buffers(setup["nlist"].astype(np.intc).copy(),
-                         setup["n_neigh"].astype(np.intc).copy(), k, s0,
-                         None, z(), z(), z(), z(), z(), np.zeros(n), None, 1,
-                         1)
-    for t in range(steps):
-        integ(mags[t], 0.0 if fmags is None else fmags[t])
-    u, _, _, force, _, damage, nlist, n_neigh = integ.write(
-        None, None, None, None, None, None, None, None)
-    return u, force, damage, nlist, n_neigh
 
 
 def _same(got, want):
@@ -72,39 +52,11 @@ def test_regression_plate(golden, ref, fused):
     assert np.allclose(got[2], golden["euler_damage"])
 
 
-def _breaking_lattice():
-    from probabilistic_peridynamics_gb300.model import (build_family,
-                                                        neighbour_pairs)
-    from tests.gpu_helpers import pull_bcs
-    rng = np.random.default_rng(11)
-    nx, ny, nz = 9, 8, 5
-    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz),
-                             indexing="ij")
-    coords = np.stack([ii.ravel(), jj.ravel(), kk.ravel()], 1).astype(float)
-    coords += rng.uniform(-0.05, 0.05, coords.shape)
-    n = coords.shape[0]
-    family, nlist, _ = build_family(n, neighbour_pairs(coords, 2.2),
-                                    pow2=False)
-    # shuffle each row (the KD-tree order of the reference is not sorted)
-    for i in range(n):
-        nlist[i, :family[i]] = rng.permutation(nlist[i, :family[i]])
-    bc_types, bc_values = pull_bcs(coords, 0, width=0.1)
-    fct = np.zeros((n, 3), dtype=np.intc)
-    fcv = np.zeros((n, 3))
-    top = coords[:, 2] > nz - 1.2
-    fct[top, 2] = 1
-    fcv[top, 2] = -1.0 / max(int(top.sum()), 1)
-    return dict(coords=coords, volume=rng.uniform(0.8, 1.2, n),
-                family=family, nlist=nlist, n_neigh=family.copy(),
-                bc_types=bc_types, bc_values=bc_values, force_bc_types=fct,
-                force_bc_values=fcv)
-
-
 @pytest.mark.parametrize("fused", [True, False])
 def test_breaking_lattice_with_force_boundaries(ref, fused):
     """Bonds break in tension (pulled faces) and in compression (the
     loaded top face) and are swap-removed from both rows, many per row."""
-    setup = _breaking_lattice()
+    setup = breaking_lattice()
     steps = 60
     mags = 2e-3 * np.arange(1, steps + 1)
     fmags = 0.05 * np.arange(1, steps + 1)

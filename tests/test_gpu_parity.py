@@ -16,8 +16,8 @@ import pytest
 from oracle import cl_step
 from tests import known_answers
 from tests.conftest import cuda_available
-from tests.gpu_helpers import (lattice, pull_bcs, rel_err, run_integrator,
-                               run_oracle)
+from tests.gpu_helpers import (breaking_setup, lattice, pull_bcs, rel_err,
+                               run_integrator, run_oracle)
 from tests.plate_setup import (BOND_STIFFNESS, CRITICAL_STRETCH, DISP_MAGS,
                                DT, STEPS)
 
@@ -173,26 +173,12 @@ def test_plate_goldens(plate, golden, kind, mode):
 
 
 # ------------------------------------------------ breaking 3-D lattice
-def _breaking_setup(kind, nx=10, ny=8, nz=4):
-    coords, volume, horizon, family, nlist, n_neigh = lattice(nx, ny, nz,
-                                                              1.0)
-    bc_types, bc_values = pull_bcs(coords, 0)
-    n = coords.shape[0]
-    return dict(coords=coords, volume=volume, family=family, nlist=nlist,
-                n_neigh=n_neigh, bc_types=bc_types, bc_values=bc_values,
-                force_bc_types=np.zeros((n, 3), dtype=np.intc),
-                force_bc_values=np.zeros((n, 3)),
-                densities=None if kind == "euler" else np.full((n, 3), 50.0),
-                nnodes=n, max_neigh=nlist.shape[1], k=0.01, s0=0.02,
-                dt=0.5 if kind == "euler" else 1.0)
-
-
 @pytest.mark.parametrize("kind", list(_KINDS))
 @pytest.mark.parametrize("mode", ["plain", "fused64", "mixed"])
 def test_breaking_lattice(kind, mode):
     """Load-induced breaking on a 320-node lattice, 60 steps."""
     import probabilistic_peridynamics_gb300 as pp
-    setup = _breaking_setup(kind)
+    setup = breaking_setup(kind)
     steps = 60
     mags = 3e-3 * np.arange(1, steps + 1)
     cls = getattr(pp, _KINDS[kind])
@@ -217,7 +203,7 @@ def test_breaking_lattice(kind, mode):
 # ---------------------------------------- n-linear, bond types, corrections
 def _nlinear_setup(kind, corrections):
     from probabilistic_peridynamics_gb300.model import Model
-    setup = _breaking_setup(kind, 10, 6, 4)
+    setup = breaking_setup(kind, 10, 6, 4)
     coords, nlist = setup["coords"], setup["nlist"]
     n, mn = nlist.shape
     mid = coords[:, 0].max() / 2
@@ -324,7 +310,7 @@ def test_model_simulate_plate(golden, tmp_path):
 def test_model_restart():
     """Two 1-step simulates equal one 2-step simulate (test_model.py:1628)."""
     import probabilistic_peridynamics_gb300 as pp
-    setup = _breaking_setup("euler")
+    setup = breaking_setup("euler")
     mags = np.linspace(0, 0.00001 * 99 / 2, 100)
     for fused in (False, True):
         model = _lattice_model(pp.EulerCUDA(dt=setup["dt"], fused=fused),
@@ -363,7 +349,7 @@ def _lattice_model(integ, setup, tmp=None):
 def test_fused_run_graph_matches_steps():
     """pp_fused_run (graph replay) == step-by-step calls, bit for bit."""
     import probabilistic_peridynamics_gb300 as pp
-    setup = _breaking_setup("velocity_verlet")
+    setup = breaking_setup("velocity_verlet")
     steps = 70
     mags = 3e-3 * np.arange(1, steps + 1)
     for precision in ("float64", "mixed"):
@@ -420,7 +406,7 @@ def test_force_boundary_conditions(kind, mode):
     ``_set_boundary_conditions`` spreads it, ``peripy/model.py:1194-1209``)
     ramped over the steps, the x-min face clamped; bonds break under it."""
     import probabilistic_peridynamics_gb300 as pp
-    setup = _breaking_setup(kind)
+    setup = breaking_setup(kind)
     coords, vol = setup["coords"], setup["volume"]
     n = coords.shape[0]
     right = coords[:, 0] >= coords[:, 0].max() - 1e-9
@@ -462,7 +448,7 @@ def test_nonuniform_volumes_and_densities(kind, mode):
     """Node volumes (bond weights k*vol_j) and densities that differ per
     node and per component, with breaking."""
     import probabilistic_peridynamics_gb300 as pp
-    setup = _breaking_setup(kind)
+    setup = breaking_setup(kind)
     n = setup["nnodes"]
     rng = np.random.default_rng(11)
     setup["volume"] = rng.uniform(0.7, 1.3, n)
