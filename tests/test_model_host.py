@@ -191,7 +191,8 @@ def test_boundary_conditions_and_tips(mesh, golden):
                is_tip=tip)
     x = m.coords[:, 0]
     left, right = x < 0.1, x > 0.9
-    assert np.all(m.bc_types[left, :2] == 1) and np.all(m.bc_types[left, 2] == 0)
+    assert np.all(m.bc_types[left, :2] == 1)
+    assert np.all(m.bc_types[left, 2] == 0)
     assert np.all(m.bc_values[left, 0] == -1.0)
     assert np.all(m.bc_types[~left] == 0)
     # force boundary values: F / volume[i], spread over the force nodes
