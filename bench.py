@@ -680,7 +680,8 @@ def load_peaks():
 
 def load_traffic():
     """DRAM bytes per launch of the fused kernel from the committed ncu
-    summary (``profiles/*traffic*.txt``: a ``dram_bytes_per_launch N`` line)."""
+    summary (``profiles/*traffic*.txt``: a ``dram_bytes_per_launch N``
+    line)."""
     for p in sorted((ROOT / "profiles").glob("*traffic*.txt")):
         for line in p.read_text().splitlines():
             if line.startswith("dram_bytes_per_launch"):

@@ -207,9 +207,10 @@ class BatchedSimulation:
         """Per-instance ``(u, ud, damage, nlist, n_neigh)``."""
         b = self.batch
         z = lambda: np.zeros((b.nnodes, 3))  # noqa: E731
-        u, ud, udd, force, body, damage, nlist, n_neigh = self.integrator.write(
-            z(), z(), z(), z(), z(), np.zeros(b.nnodes), b.nlist.copy(),
-            b.n_neigh.copy())
+        (u, ud, udd, force, body, damage, nlist,
+         n_neigh) = self.integrator.write(
+             z(), z(), z(), z(), z(), np.zeros(b.nnodes), b.nlist.copy(),
+             b.n_neigh.copy())
         return list(zip(b.split(u), b.split(ud), b.split(damage),
                         b.split(nlist, "nlist"), b.split(n_neigh)))
 

@@ -64,7 +64,8 @@ def build(force=False, verbose=False):
         src, obj = job
         extra = [f for prefix, flags in UNIT_FLAGS.items()
                  if src.name.startswith(prefix) for f in flags]
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", str(src), "-o",
+               str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
         res = subprocess.run(cmd, capture_output=True, text=True)

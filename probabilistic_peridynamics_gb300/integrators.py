@@ -639,7 +639,8 @@ class _CUDAIntegrator(Integrator):
         if host is None:
             return dev.cpu().numpy()
         np_dtype = {torch.float64: np.float64, torch.float32: np.float32,
-                    torch.int32: np.int32, torch.int64: np.int64}.get(dev.dtype)
+                    torch.int32: np.int32,
+                    torch.int64: np.int64}.get(dev.dtype)
         if (isinstance(host, np.ndarray) and host.flags.c_contiguous
                 and host.flags.writeable and host.size == dev.numel()
                 and host.dtype == np_dtype):

@@ -94,7 +94,8 @@ def nlinear_tables(bond_stiffness, critical_stretch):
         raise ValueError("bond_stiffness and critical_stretch differ in shape")
     c = np.zeros_like(k)
     for r in range(1, k.shape[1]):
-        c[:, r] = c[:, r - 1] + k[:, r - 1] * s[:, r - 1] - k[:, r] * s[:, r - 1]
+        c[:, r] = (c[:, r - 1] + k[:, r - 1] * s[:, r - 1]
+                   - k[:, r] * s[:, r - 1])
     return k, s, c
 
 
