@@ -648,13 +648,16 @@ class _CUDAIntegrator(Integrator):
             # writes it directly instead of through the driver's staging
             # buffers (on the GPU machine: ~130 against ~20 GB/s into fresh
             # pages); if it cannot be registered it is copied as it is.
+            # Memory that is pinned already (a view of a pinned tensor) is
+            # left as it is: registering it again would fail.
+            target = torch.from_numpy(host.reshape(-1))
             registered = False
-            if host.nbytes >= _REGISTER_BYTES:
+            if host.nbytes >= _REGISTER_BYTES and not target.is_pinned():
                 cudart = torch.cuda.cudart()
                 registered = int(cudart.cudaHostRegister(
                     host.ctypes.data, host.nbytes, 0)) == 0
             try:
-                torch.from_numpy(host.reshape(-1)).copy_(dev.reshape(-1))
+                target.copy_(dev.reshape(-1))
             finally:
                 if registered:
                     cudart.cudaHostUnregister(host.ctypes.data)

@@ -154,3 +154,51 @@ def test_simulate_with_writes_matches_host_path(kind, precision, golden,
         name = f"U_{step}.vtk"
         assert (dev_path / name).read_bytes() == \
             (host_path / name).read_bytes()
+
+
+def test_write_into_registered_and_pinned_arrays(monkeypatch):
+    """Integrator.write page-locks large host arrays for the copy (every
+    array here, with the size threshold at 0) and leaves memory that is
+    pinned already alone; the values are those of an ordinary copy and no
+    CUDA error is left behind."""
+    import torch
+    import probabilistic_peridynamics_gb300 as pp
+    from probabilistic_peridynamics_gb300 import integrators
+    from tests.gpu_helpers import breaking_setup
+    setup = breaking_setup("velocity_verlet")
+    n = setup["nnodes"]
+    outs = []
+    for mode in ("plain", "registered", "pinned"):
+        monkeypatch.setattr(integrators, "_REGISTER_BYTES",
+                            1 << 40 if mode == "plain" else 0)
+        integ = pp.VelocityVerletCUDA(0.5, dt=setup["dt"])
+        integ.build(n, 3, setup["max_neigh"], setup["coords"],
+                    setup["volume"], setup["family"], setup["bc_types"],
+                    setup["bc_values"], setup["force_bc_types"],
+                    setup["force_bc_values"], None, None,
+                    setup["densities"])
+        z = np.zeros((n, 3))
+        integ.create_buffers(setup["nlist"].copy(), setup["n_neigh"].copy(),
+                             setup["k"], setup["s0"], None, z, z, z, z, z,
+                             np.zeros(n), None, 1, 1)
+        for t in range(20):
+            integ(3e-3 * (t + 1), 0.0)
+        if mode == "pinned":
+            bufs = [torch.zeros(n * 3, dtype=torch.float64,
+                                pin_memory=True) for _ in range(5)]
+            host = [b.numpy().reshape(n, 3) for b in bufs]
+            nl = torch.zeros(setup["nlist"].size, dtype=torch.int32,
+                             pin_memory=True).numpy().reshape(
+                                 setup["nlist"].shape)
+        else:
+            host = [np.zeros((n, 3)) for _ in range(5)]
+            nl = np.zeros_like(setup["nlist"])
+        out = integ.write(*host, np.zeros(n), nl,
+                          np.zeros(n, dtype=np.intc))
+        outs.append([np.array(a, copy=True) for a in out])
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)
+    x = torch.ones(4, device="cuda") * 2  # a launch after the writes
+    torch.cuda.synchronize()
+    assert float(x.sum()) == 8.0
