@@ -276,3 +276,35 @@ def test_simulate_argument_checks(mesh):
     m.simulate(steps=2)
     assert np.array_equal(m.initial_connectivity[0], before)
     assert m.integrator.buffers[0] is not m.initial_connectivity[0]
+
+
+def test_write_mesh_and_cached_arrays(mesh, golden, tmp_path):
+    """write_mesh (model.py:505-534) writes the nodes, the cells and the
+    point data; with write_path the set-up arrays are cached as files."""
+    from probabilistic_peridynamics_gb300.mesh import read_vtk
+    from probabilistic_peridynamics_gb300.model import read_array
+    cache = tmp_path / "cache"
+    m = _model(mesh, write_path=cache, is_density=lambda x: 2.0)
+    for name in ("volume", "family", "nlist", "n_neigh", "density"):
+        assert read_array(cache, name) is not None
+    assert np.array_equal(read_array(cache, "volume"), m.volume)
+    assert np.array_equal(read_array(cache, "nlist"),
+                          m.initial_connectivity[0])
+    out = tmp_path / "state.vtk"
+    damage = np.linspace(0.0, 1.0, m.nnodes)
+    u = np.arange(3 * m.nnodes, dtype=np.float64).reshape(-1, 3)
+    m.write_mesh(out, damage, u)
+    back = read_vtk(out)
+    assert np.array_equal(back.points, m.coords)
+    assert np.array_equal(back.cells_dict["triangle"],
+                          golden["cells_triangle"])
+    assert np.array_equal(back.cells_dict["line"], golden["cells_line"])
+    # the point data follow the cells: damage then displacements
+    raw = out.read_bytes()
+    assert b"POINT_DATA %d" % m.nnodes in raw
+    assert b"damage 1 %d double" % m.nnodes in raw
+    assert b"displacements 3 %d double" % m.nnodes in raw
+    at = raw.index(b"damage 1 %d double\n" % m.nnodes) + len(
+        b"damage 1 %d double\n" % m.nnodes)
+    got = np.frombuffer(raw[at:at + 8 * m.nnodes], dtype=">f8")
+    assert np.array_equal(got, damage)
