@@ -713,7 +713,10 @@ class Euler(Integrator):
     compact, 0-padded neighbour list this step works on; the kernels run on
     a :class:`CUDAContext` of their own (``device_context``, device 0 by
     default).  Bond types, n-linear damage, stiffness corrections and
-    densities are rejected as the reference rejects them.
+    densities are rejected as the reference rejects them.  The neighbour
+    list must be symmetric (j among the valid entries of row i exactly when
+    i is among those of row j), as every list Model builds is:
+    :meth:`create_buffers` raises ValueError otherwise.
     """
 
     def __init__(self, dt, device_context=None, fused=True):
@@ -821,6 +824,12 @@ class Euler(Integrator):
         with self.device_context.on_stream():
             self._nlist_d = self._dev(nlist, np.int32, (n, width))
             self._n_neigh_d = self._dev(n_neigh, np.int32, (n,))
+            if not self._symmetric():
+                raise ValueError(
+                    "the GPU Euler integrator needs a symmetric neighbour "
+                    "list (j among the first n_neigh[i] entries of row i "
+                    "exactly when i is among those of row j), as Model "
+                    "builds it; this list is not")
             self._u_d = self._dev(u, np.float64, (n, 3))
             self._force_d = self._dev(force, np.float64, (n, 3))
             self._damage_d = torch.empty(n, dtype=torch.float64,
@@ -835,6 +844,24 @@ class Euler(Integrator):
                     _ptr(self._coords_d), _ptr(self._nlist_d), n, width,
                     _ptr(self._l0_d), self.device_context.stream_handle),
                     "pp_bond_lengths")
+
+    def _symmetric(self):
+        """Is j a valid entry of row i exactly when i is one of row j?
+        (Compares the sorted pairs (i, j) with the sorted pairs (j, i).)"""
+        import torch
+        n, w = self.nnodes, self._width
+        if n == 0 or w == 0:
+            return True
+        dev = self.device_context.device
+        counts = self._n_neigh_d.clamp(0, w)
+        valid = (torch.arange(w, device=dev)[None, :] < counts[:, None])
+        j = self._nlist_d[valid].long()
+        if bool(((j < 0) | (j >= n)).any()):
+            return False
+        i = torch.arange(n, device=dev)[:, None].expand(n, w)[valid].long()
+        forward = torch.sort(i * n + j).values
+        backward = torch.sort(j * n + i).values
+        return bool(torch.equal(forward, backward))
 
     def __call__(self, displacement_bc_magnitude, force_bc_magnitude):
         """One step: break bonds, bond forces, Euler update

@@ -101,3 +101,65 @@ def test_model_simulate(golden, tmp_path, ref):
                                BOND_STIFFNESS, CRITICAL_STRETCH)
     _same((u, force, damage, nlist, n_neigh), want)
     assert np.allclose(u, golden["euler_u"])
+
+
+def test_known_answers_of_the_cython_functions():
+    """The reference's own known answers for peridynamics.pyx
+    (test_peridynamics.py:7-57): damage, and break_bonds on the 5-node
+    case with its expected compacted rows (critical strain 1.0)."""
+    import probabilistic_peridynamics_gb300 as pp
+    r0 = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0],
+                   [2.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    nl = np.array([[1, 2, 4], [0, 3, 0], [0, 0, 0], [1, 0, 0], [0, 0, 0]],
+                  dtype=np.intc)
+    n_neigh = np.array([3, 2, 1, 1, 1], dtype=np.intc)
+    r = np.array([[0.0, 0.0, 0.0], [2.0, 0.0, 0.0], [0.0, 1.0, 0.0],
+                  [3.0, 0.0, 0.0], [0.0, 0.0, 2.0]])
+    n = 5
+    integ = pp.Euler(1.0)
+    z = np.zeros((n, 3))
+    integ.build(n, 3, 3, r0, np.ones(n), n_neigh.copy(),
+                np.ones((n, 3), dtype=np.intc), z, np.zeros((n, 3), np.intc),
+                z, None, None, None)
+    # every displacement is a boundary value: one step moves r0 to r, and
+    # the next step's breaks see r
+    integ.create_buffers(nl.copy(), n_neigh.copy(), 1.0, 1.0, None,
+                         np.zeros((n, 3)), z, z, z, z, np.zeros(n), None, 1,
+                         1)
+    integ._bc_values_d.copy_(torch_tensor(r - r0, integ))
+    integ(1.0, 0.0)  # u := r - r0; the breaks of this step saw u = 0
+    integ(1.0, 0.0)  # breaks at r
+    _, _, _, _, _, damage, got_nl, got_nn = integ.write(*[None] * 8)
+    assert np.array_equal(got_nl, [[2, 2, 4], [3, 3, 0], [0, 0, 0],
+                                   [1, 0, 0], [0, 0, 0]])
+    assert np.array_equal(got_nn, [1, 1, 1, 1, 0])
+    family = n_neigh.astype(np.float64)
+    assert np.array_equal(damage, (family - got_nn) / family)
+
+
+def torch_tensor(a, integ):
+    import torch
+    return torch.as_tensor(a, device=integ.device_context.device)
+
+
+def test_asymmetric_list_is_rejected():
+    """The 3-node list of the reference's force test (test_peridynamics.py
+    :92-133) is not symmetric (node 2's row holds itself, node 1's holds
+    node 2): the GPU Euler refuses it rather than differ."""
+    import probabilistic_peridynamics_gb300 as pp
+    n = 3
+    r0 = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [1.0, 1.0, 0.0]])
+    nl = np.array([[1, 0], [0, 2], [2, 0]], dtype=np.intc)
+    n_neigh = np.array([1, 2, 1], dtype=np.intc)
+    integ = pp.Euler(1.0)
+    z = np.zeros((n, 3))
+    integ.build(n, 3, 2, r0, np.full(n, 0.16666667), n_neigh.copy(),
+                np.zeros((n, 3), np.intc), z, np.zeros((n, 3), np.intc), z,
+                None, None, None)
+    with pytest.raises(ValueError, match="symmetric"):
+        integ.create_buffers(nl, n_neigh, 1.0, 1.0, None, z, z, z, z, z,
+                             np.zeros(n), None, 1, 1)
+    # the same bonds listed from both ends are accepted
+    sym = np.array([[1, 0], [0, 2], [1, 0]], dtype=np.intc)
+    integ.create_buffers(sym, n_neigh, 1.0, 1.0, None, z, z, z, z, z,
+                         np.zeros(n), None, 1, 1)
