@@ -170,7 +170,10 @@ def build_workload(pow2=True):
                 bonds=int(family.sum()), crack_pairs=int(len(pairs)))
 
 
-def make_integrator(w, precision, fused, context=None, autotune=True):
+def make_integrator(w, precision, fused, context=None, autotune=True,
+                    u0=None):
+    """A Velocity-Verlet integrator on the plate, from rest at ``u0``
+    (default: undeformed)."""
     import probabilistic_peridynamics_gb300 as pp
     integ = pp.VelocityVerletCUDA(DAMPING, dt=DT, precision=precision,
                                   fused=fused, context=context,
@@ -181,75 +184,135 @@ def make_integrator(w, precision, fused, context=None, autotune=True):
                 w["densities"])
     n = w["nnodes"]
     z = np.zeros((n, 3))
-    integ.create_buffers(w["nlist"], w["n_neigh"], w["k"], w["s0"], None, z,
-                         z, z, z, z, np.zeros(n), None, 1, 1)
+    integ.create_buffers(w["nlist"], w["n_neigh"], w["k"], w["s0"], None,
+                         z if u0 is None else u0, z, z, z, z, np.zeros(n),
+                         None, 1, 1)
     return integ
+
+
+#: Fracture variant of the plate: released at rest from a uniform strain
+#: FRACTURE_EPS0 along x (u_x = eps0 (x - 0.5)), the faces held at that
+#: strain and pulled on at PULL_RATE per step.  The bonds cut by the
+#: pre-crack leave the crack faces unbalanced; the release waves and the
+#: free surfaces overload bonds near the crack tip and along the faces:
+#: about 270,000 bonds break within 100 steps and 380,000 within 300.
+FRACTURE_EPS0 = 0.004
+
+
+def fracture_state(w, eps0=FRACTURE_EPS0):
+    """``(u0, mags(steps))`` of the fracture variant."""
+    x = w["coords"][:, 0]
+    u0 = np.zeros((w["nnodes"], 3))
+    u0[:, 0] = eps0 * (x - 0.5)
+    face = eps0 * (x.max() - 0.5)
+
+    def mags(steps):
+        return face + PULL_RATE * np.arange(1, steps + 1)
+    return u0, mags
 
 
 # -------------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi samples (200 ms) of SM clock and throttle reasons."""
+    """SM clock, power and throttle reasons sampled every 200 ms while the
+    timed region runs.
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
-              "clocks_event_reasons.active,"
+    Each sample is one ``nvidia-smi --query-gpu`` call that exits after
+    printing (a looping ``nvidia-smi -lms`` writing into a pipe buffers its
+    output, and stopping it loses the buffer).  Where ``nvidia-smi`` cannot
+    run, the same quantities are read through NVML (``libnvidia-ml.so.1``,
+    read-only queries).  ``errors`` records why a source gave nothing.
+    """
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,"
               "clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+             "sw_power_cap")
+    #: NVML clock-event reason bits of NAMES (nvml.h)
+    NVML_BITS = (0x8, 0x40, 0x20, 0x4)
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, period_s=0.2):
         self.gpu = gpu_index
-        self.proc = None
-        self.lines = []
+        self.period = period_s
+        self.samples = []  # (sm_mhz, max_mhz, power_w, reasons)
+        self.errors = []
+        self._stop = threading.Event()
+        self._thread = None
+        self._nvml = None
+
+    def _smi(self):
+        r = subprocess.run(
+            ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+             "--format=csv,noheader,nounits"],
+            capture_output=True, text=True, timeout=5)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvidia-smi rc {r.returncode}: "
+                               f"{r.stderr.strip()[:120]}")
+        parts = [x.strip() for x in r.stdout.strip().split(",")]
+        reasons = {n for n, f in zip(self.NAMES, parts[3:7])
+                   if f.lower().startswith("active")}
+        return float(parts[0]), float(parts[1]), float(parts[2]), reasons
+
+    def _nvml_sample(self):
+        import ctypes
+        if self._nvml is None:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                raise RuntimeError("nvmlInit failed")
+            h = ctypes.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(self.gpu,
+                                                 ctypes.byref(h)) != 0:
+                raise RuntimeError("nvmlDeviceGetHandleByIndex failed")
+            self._nvml = (lib, h)
+        lib, h = self._nvml
+        sm, mx, mw = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
+        rs = ctypes.c_ulonglong()
+        lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm))      # SM clock
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))
+        lib.nvmlDeviceGetPowerUsage(h, ctypes.byref(mw))
+        lib.nvmlDeviceGetCurrentClocksThrottleReasons(h, ctypes.byref(rs))
+        reasons = {n for n, b in zip(self.NAMES, self.NVML_BITS)
+                   if rs.value & b}
+        return float(sm.value), float(mx.value), mw.value / 1e3, reasons
+
+    def _loop(self):
+        sources = [self._smi, self._nvml_sample]
+        while not self._stop.is_set():
+            t = time.perf_counter()
+            while sources:
+                try:
+                    self.samples.append(sources[0]())
+                    break
+                except Exception as e:  # noqa: BLE001 - next source
+                    self.errors.append(f"{sources[0].__name__}: {e}"[:160])
+                    sources.pop(0)
+            if not sources:
+                return
+            self._stop.wait(max(0.0, self.period - (time.perf_counter() - t)))
 
     def start(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.gpu}",
-                 f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
-                 "-lms", "200"], stdout=subprocess.PIPE,
-                stderr=subprocess.DEVNULL, text=True)
-        except (OSError, ValueError):
-            self.proc = None
-            return
-        self.thread = threading.Thread(target=self._read, daemon=True)
-        self.thread.start()
-
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+        self._thread = threading.Thread(target=self._loop, daemon=True)
+        self._thread.start()
 
     def stop(self):
-        if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
-                    "samples": 0}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        self.thread.join(timeout=2)
-        sm, smax, reasons, power = [], [], set(), []
-        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
-                 "sw_power_cap")
-        for line in self.lines:
-            parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1].split()[0]))
-                smax.append(float(parts[2].split()[0]))
-                power.append(float(parts[3].split()[0]))
-            except (ValueError, IndexError):
-                continue
-            for name, flag in zip(names, parts[5:9]):
-                if flag.lower().startswith("active"):
-                    reasons.add(name)
-        loaded = [s for s, p in zip(sm, power) if p > 300.0] or sm
+        self._stop.set()
+        if self._thread is not None:
+            self._thread.join(timeout=10)
+        sm = [s[0] for s in self.samples]
+        loaded = [s[0] for s in self.samples if s[2] > 300.0] or sm
+        reasons = set()
+        for s in self.samples:
+            reasons |= s[3]
         return {"sm_mhz": statistics.median(loaded) if loaded else None,
-                "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm),
-                "power_w_max": max(power) if power else None}
+                "sm_max_mhz": max(s[1] for s in self.samples)
+                if self.samples else None,
+                "reasons": sorted(reasons), "samples": len(self.samples),
+                "samples_under_load": sum(s[2] > 300.0 for s in self.samples),
+                "power_w_max": max(s[2] for s in self.samples)
+                if self.samples else None,
+                "errors": self.errors[:3]}
 
 
 # ------------------------------------------------------------ measurements
@@ -268,9 +331,11 @@ def job_throughput(world, bonds, steps, ms):
     return world * bonds * steps / (ms * 1e-3)
 
 
-def time_steps(integ, steps, warmup, torch, dist=None, rate=PULL_RATE):
-    """Device time of exactly ``steps`` fused steps (graph replays)."""
-    dm = torch.as_tensor(rate * np.arange(1, warmup + steps + 1),
+def time_steps(integ, steps, warmup, torch, dist=None, rate=PULL_RATE,
+               offset=0.0):
+    """Device time of exactly ``steps`` fused steps (graph replays); the
+    displacement magnitudes are ``offset + rate * k``."""
+    dm = torch.as_tensor(offset + rate * np.arange(1, warmup + steps + 1),
                          dtype=torch.float64, device=integ.context.device)
     fm = torch.zeros_like(dm)
     stream = integ.context.stream
@@ -378,6 +443,70 @@ def accuracy(w, steps, torch):
     return {"steps": steps, "disp_rel_err_vs_fp64": err,
             "mask_flips_vs_fp64": flips, "bonds_broken_fp64": broken,
             "max_abs_u": float(np.max(np.abs(u64)))}
+
+
+def _write_all(integ, w):
+    n = w["nnodes"]
+    z = [np.zeros((n, 3)) for _ in range(5)]
+    return integ.write(*z, np.zeros(n), w["nlist"].copy(),
+                       w["n_neigh"].copy())
+
+
+def accuracy_fracture(w, torch, checkpoints=(100, 300)):
+    """The fracture variant: mixed vs FP64 fused from the same pre-strained
+    state, compared at each checkpoint step (bonds broken, mask flips,
+    intact counts, displacement error)."""
+    u0, mags = fracture_state(w)
+    steps = max(checkpoints)
+    m = mags(steps)
+    out = {}
+    for precision in ("float64", "mixed"):
+        integ = make_integrator(w, precision, True, u0=u0)
+        done, snaps = 0, {}
+        for c in checkpoints:
+            integ._run(m, np.zeros(steps), done, c - done)
+            done = c
+            snaps[c] = _write_all(integ, w)
+        out[precision] = snaps
+        del integ
+        torch.cuda.empty_cache()
+    res = {"eps0": FRACTURE_EPS0, "pull_rate": PULL_RATE}
+    initial = int(np.sum(w["nlist"] != -1))
+    for c in checkpoints:
+        a, b = out["float64"][c], out["mixed"][c]
+        res[f"step_{c}"] = {
+            "bonds_broken_fp64": initial - int(np.sum(a[6] != -1)),
+            "mask_flips_vs_fp64": int(np.sum(a[6] != b[6])),
+            "n_neigh_equal": bool(np.array_equal(a[7], b[7])),
+            "disp_rel_err_vs_fp64": float(np.max(np.abs(b[0] - a[0])) /
+                                          np.max(np.abs(a[0]))),
+            "max_abs_u": float(np.max(np.abs(a[0])))}
+    return res
+
+
+def time_fracture(w, steps, torch, ctx=None, settle=100):
+    """The mixed step in the fractured state: ``settle`` steps from the
+    pre-strained state (most of the breaking happens there), then
+    ``steps`` graph-replayed steps timed while bonds keep breaking."""
+    u0, mags = fracture_state(w)
+    integ = make_integrator(w, "mixed", True, context=ctx, u0=u0)
+    m = mags(settle)
+    integ._run(m, np.zeros(settle), 0, settle)
+    before = _write_all(integ, w)
+    ms = time_steps(integ, steps, 0, torch, offset=float(m[-1]))
+    kernel_ms = time_kernel_launches(integ, 50, torch,
+                                     first_mag=float(m[-1]) +
+                                     PULL_RATE * (steps + 1))
+    after = _write_all(integ, w)
+    del integ
+    torch.cuda.empty_cache()
+    initial = int(np.sum(w["nlist"] != -1))
+    return {"bond_updates_per_s": w["bonds"] * steps / (ms * 1e-3),
+            "ms_per_step": ms / steps, "kernel_ms": kernel_ms,
+            "timed_steps": steps, "after_steps": settle,
+            "bonds_broken_before": initial - int(np.sum(before[6] != -1)),
+            "bonds_broken_after": initial - int(np.sum(after[6] != -1)),
+            "eps0": FRACTURE_EPS0}
 
 
 def e2e_simulate(w, torch):
@@ -1135,14 +1264,16 @@ def main():
     ctx = CUDAContext(local)
     w = build_workload()
     integ = make_integrator(w, "mixed", True, context=ctx)
+    # clocks sampled from the warm-up through the per-launch timing (the
+    # timed region alone can be shorter than one 200 ms sample)
     clocks = ClockSampler(local)
     clocks.start()
     ms = time_steps(integ, args.steps, args.warmup, torch, dist)
-    clk = clocks.stop()
     ms = job_time_ms(ms, dist, torch, "cuda")
     ms_per_step = ms / args.steps
     value = job_throughput(world, w["bonds"], args.steps, ms)
     kernel_ms = time_kernel_launches(integ, 200, torch)
+    clk = clocks.stop()
     tuning = integ.tuning
     variant = int(integ._fargs.variant)
     launches = args.steps + (args.steps // 16 + 1
@@ -1181,8 +1312,10 @@ def main():
     variants["euler_cython_gpu"] = time_cython_euler(w, args.fp64_steps,
                                                      torch)
 
+    variants["fused_mixed_fracture"] = time_fracture(w, 20, torch, ctx)
     acc = accuracy(w, args.accuracy_steps, torch) if args.accuracy_steps \
         else None
+    acc_fracture = accuracy_fracture(w, torch)
     e2e = None if args.no_e2e else e2e_simulate(w, torch)
     cpu = None if args.no_cpu else cpu_baseline()
 
@@ -1210,6 +1343,7 @@ def main():
                      "peak_source": ("measured" if peaks else "fallback")},
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
         "clocks": clk, "variants": variants, "accuracy": acc,
+        "accuracy_fracture": acc_fracture,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

@@ -20,13 +20,14 @@
 #ifndef PP_GB300_H
 #define PP_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
 extern "C" {
 #endif
 
-#define PP_ABI_VERSION 2
+#define PP_ABI_VERSION 3
 
 /* Status codes. */
 #define PP_SUCCESS                  0
@@ -57,6 +58,9 @@ extern "C" {
 #define PP_STATUS_OK                0
 #define PP_STATUS_COPY_TIMEOUT      1  /* a wait for an asynchronous copy ran
                                           out: the step's results are invalid */
+#define PP_STATUS_BAD_TILING        2  /* a tile exceeded PP_TILE_NODES_MAX or
+                                          its halo capacity: it was skipped,
+                                          the step's results are invalid   */
 
 /* Flags of the fused step. */
 #define PP_FLAG_COMPENSATED         1  /* PP_MIXED only: compensated FP32 force
@@ -182,6 +186,63 @@ int pp_update_displacement_velocity_verlet(
 /* pp_mixed_export() writes the reference-layout f64 arrays.                */
 /* ------------------------------------------------------------------------ */
 
+/* ------------------------------------------------------------------------ */
+/* Tiled layout of the PP_MIXED step (no counterpart in the reference,      */
+/* whose kernels gather every neighbour from global memory).                */
+/*                                                                          */
+/* The nodes are renumbered internally ("internal order": internal node i  */
+/* is reference node perm[i]) and cut into tiles, ranges [tile_start[t],    */
+/* tile_start[t+1]) of at most PP_TILE_NODES_MAX internal nodes.  The halo  */
+/* of a tile is the ascending list of internal nodes its bonds reach (its   */
+/* own nodes included), at most halo_cap long.  A step stages each tile's   */
+/* halo records in shared memory once and gathers every bond of the tile   */
+/* from there.  Row i holds the bonds of internal node i as 16-bit indices  */
+/* into its tile's halo ("entries"), 0xFFFF for broken bonds and padding,   */
+/* in the reference row's slot order, CSR-packed: row i occupies entries    */
+/* [16 row_off[i], 16 row_off[i+1]), its length the number of its intact   */
+/* slots rounded up to 16.  Row entry p = 16 m + 8 h + l (l < 8, h < 2) is  */
+/* stored at position 16 m + 2 l + h of the row, so that lane l of a node's */
+/* eight lanes reads its entries 16 m + l and 16 m + 8 + l with one 32-bit  */
+/* load.  Any permutation and any cut into ranges gives the same results;   */
+/* spatial locality of the tiles only makes the step faster.                */
+/*                                                                          */
+/* The caller allocates every array and chooses perm and tile_start;       */
+/* pp_tile_halos and pp_tile_rows fill the rest from the reference layouts. */
+/* ------------------------------------------------------------------------ */
+
+#define PP_TILE_NODES_MAX           128   /* internal nodes per tile       */
+#define PP_TILE_HALO_MAX            4096  /* largest halo_cap              */
+
+typedef struct pp_tiling {
+    int32_t ntiles;
+    int32_t halo_cap;          /* halo capacity per tile, 1..PP_TILE_HALO_MAX */
+    const int32_t* perm;       /* (nnodes) internal -> reference node      */
+    const int32_t* inv;        /* (nnodes) reference -> internal node      */
+    const int32_t* tile_start; /* (ntiles + 1), tile_start[0] = 0,
+                                  tile_start[ntiles] = nnodes             */
+    int32_t* halo;             /* (ntiles * halo_cap) internal nodes       */
+    int32_t* halo_count;       /* (ntiles) halo lengths (pp_tile_halos)    */
+    int32_t* own_off;          /* (ntiles) halo index of the tile's first node */
+    int32_t* row_off;          /* (nnodes + 1) row offsets, units of 16 entries */
+    uint16_t* entry;           /* (16 row_off[nnodes]) halo index per entry */
+    uint8_t* slot;             /* same length: the entry's slot in the
+                                  reference row, 0xFF for padding         */
+    uint8_t* bond_type;        /* same length, or NULL without bond types  */
+    uint8_t* regime;           /* same length, or NULL without bond types  */
+    float* correction;         /* same length, or NULL without stiffness
+                                  corrections (rounded to float)          */
+    double* r0;                /* (nnodes, 3) internal order               */
+    double* bc_values;         /* (nnodes, 3) internal order               */
+    double* fc_values;         /* (nnodes, 3) internal order               */
+    int32_t* node_instance;    /* (nnodes) internal order, or NULL         */
+    int32_t* n_neigh;          /* (nnodes) internal order: intact bonds
+                                  after a step                            */
+    int32_t* sched;            /* two device words, zero before the first
+                                  step (pp_tile_rows zeroes them); the step
+                                  hands out tiles with them and leaves them
+                                  zero                                    */
+} pp_tiling;
+
 typedef struct pp_fused_args {
     int32_t nnodes;
     int32_t max_neigh;             /* power of two, 1..1024               */
@@ -251,6 +312,13 @@ typedef struct pp_fused_args {
     double pos_scale;
     double min_bond;               /* smallest |xi| over the bonds (pp_bond_extent) */
     double pos_origin[3];
+    /* PP_MIXED: the tiled layout (host pointer to a struct of device
+       pointers), or NULL for the untiled kernel.  With a tiling the mixed
+       node state (rec, ulo, vel, acc, frc, rho32, nflags) is in internal
+       order and the neighbour list, regimes, n_neigh and stiffness
+       corrections are read and written through the tiling; pp_mixed_pack
+       and pp_mixed_export convert from and to the reference layouts. */
+    const pp_tiling* tiling;
 } pp_fused_args;
 
 /* One fused step reading state slot `parity`; magnitudes of the
@@ -296,9 +364,23 @@ int pp_bond_lengths(const double* r0, const int32_t* nlist, int32_t nnodes,
 int pp_mixed_pack(const pp_fused_args* args, int32_t parity, void* stream);
 
 /* Writes the reference layouts u[parity], ud, udd, force, body_force
- * (float64) from the PP_MIXED state slot `parity`.  Called by write()
- * (peripy/integrators.py:285-300). */
+ * (float64) from the PP_MIXED state slot `parity`; with a tiling also the
+ * -1 of every bond broken since pp_tile_rows into nlist, and regimes.
+ * Called by write() (peripy/integrators.py:285-300). */
 int pp_mixed_export(const pp_fused_args* args, int32_t parity, void* stream);
+
+/* Tiled layout, first part: from the reference nlist (args->nlist,
+ * args->max_neigh) and t->perm, inv, tile_start, ntiles, halo_cap, writes
+ * halo, halo_count, own_off and row_off.  A tile whose halo would exceed
+ * halo_cap gets halo_count = its halo's length (> halo_cap) and no halo:
+ * the caller splits it and calls again.  On return (after the stream),
+ * row_off[nnodes] is the number of 16-entry blocks the rows need. */
+int pp_tile_halos(const pp_fused_args* args, const pp_tiling* t, void* stream);
+
+/* Tiled layout, second part (every halo_count <= halo_cap): writes entry,
+ * slot, bond_type, regime, correction (those not NULL), the internal-order
+ * copies r0, bc_values, fc_values, node_instance, and zeroes sched. */
+int pp_tile_rows(const pp_fused_args* args, const pp_tiling* t, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Neighbour families (set-up).  Replace the host KD-tree search of         */
@@ -389,6 +471,14 @@ int pp_cy_update_displacement(double* u, const double* bc_values, const int32_t*
                               void* stream);
 int pp_cy_damage(const int32_t* n_neigh, const int32_t* family, int32_t nnodes, double* damage,
                  void* stream);
+/* The precondition of the calls above, checked on the device before a
+ * list is used (no counterpart in the reference, whose sequential loops
+ * accept any list): *bad (one caller-allocated device word, zeroed here)
+ * receives the number of entries j of a row i (among its first n_neigh[i])
+ * that lie outside [0, nnodes) or whose row does not hold i exactly as
+ * often as row i holds j; 0 means the list is symmetric. */
+int pp_cy_check_symmetric(const int32_t* nlist, const int32_t* n_neigh, int32_t nnodes,
+                          int32_t width, uint32_t* bad, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Write-step sums.  Replace the NumPy reductions Model.simulate runs at    */
@@ -550,14 +640,33 @@ int pp_adjoint_backward(const pp_adjoint_args* args, const double* u,
  * PP_ERROR_TOO_LARGE.  It calls no cudaMalloc, cudaFree or other allocating
  * routine.
  *
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress, with that device current); make that first call
+ * The schedule is copied with cudaMemcpyAsync on `stream`.  From pageable
+ * host memory the copy completes before the call returns; from page-locked
+ * (pinned or registered) memory it is truly asynchronous, so the caller
+ * must keep disp_mags[0..nsteps) and force_mags[0..nsteps) allocated and
+ * unchanged until the stream has executed the call.  A pageable source
+ * cannot be captured into a CUDA graph; make no claim here beyond that.
+ *
+ * The first call in each CUDA context looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current) and caches it together
+ * with the context's unique ID, so after a device reset or a re-created
+ * primary context the next call looks it up again; make that first call
  * before any stream capture.  All calls share the one array: calls whose
  * work overlaps on the GPU (different streams, or host threads) race on it
  * and must be serialised by the caller. */
 int pp_fused_run_static(const pp_fused_args* args, int32_t parity,
                         int64_t nsteps, const double* disp_mags,
                         const double* force_mags, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Host memory.  Page-lock (cudaHostRegister) and release a caller host     */
+/* array, used for the device-to-host copies of write().  No counterpart in */
+/* the reference (pyopencl copies into pageable arrays).  A failed          */
+/* registration returns PP_ERROR_CUDA and leaves no pending error in the   */
+/* library's runtime; the array can still be copied as pageable memory.    */
+/* ------------------------------------------------------------------------ */
+int pp_host_register(void* ptr, size_t bytes);
+int pp_host_unregister(void* ptr);
 
 /* Copies the status word of the last pp_fused_run_static call on `stream`
  * (PP_STATUS_*) to *status (host memory) and waits for the stream.  No

@@ -3,7 +3,9 @@ INFRASTRUCTURE: the checker and the timed CPU baseline, never the product).
 
 Recipe
 ------
-1. Where the reference checkout exists (``/root/reference``, read-only),
+1. Where the reference checkout exists (read-only; the directory named by
+   the ``PP_REFERENCE`` environment variable or the ``reference`` argument,
+   else a ``reference`` directory beside this repository's checkout),
    Cython translates ``peripy/peridynamics.pyx``, ``peripy/correction.pyx``,
    ``peripy/create_crack.pyx`` and ``peripy/spatial.pyx`` (which the first
    two cimport through ``spatial.pxd``) from where they lie into C files under
@@ -36,7 +38,10 @@ REF_OUT = HERE / "_ref"
 SRC = REF_OUT / "src"
 PKG = REF_OUT / "peripy"
 MODULES = ("spatial", "peridynamics", "correction", "create_crack")
-DEFAULT_REFERENCE = pathlib.Path("/root/reference")
+#: The reference checkout: ``$PP_REFERENCE``, else ``reference`` beside the
+#: repository's own checkout.
+DEFAULT_REFERENCE = pathlib.Path(
+    os.environ.get("PP_REFERENCE") or HERE.parent.parent / "reference")
 
 
 def _ext_suffix():

@@ -32,6 +32,9 @@ PP_FLAG_COMPENSATED = 1
 PP_MIXED_VARIANTS = 3
 PP_STATUS_OK = 0
 PP_STATUS_COPY_TIMEOUT = 1
+PP_STATUS_BAD_TILING = 2
+PP_TILE_NODES_MAX = 128
+PP_TILE_HALO_MAX = 4096
 
 _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
@@ -80,6 +83,21 @@ class FusedArgs(ctypes.Structure):
         ("acc", _vp), ("frc", _vp), ("rho32", _vp), ("sc32", _vp),
         ("nflags", _vp), ("umax", _vp), ("status", _vp),
         ("pos_scale", _f64), ("min_bond", _f64), ("pos_origin", _f64 * 3),
+        ("tiling", _vp),
+    ]
+
+
+class Tiling(ctypes.Structure):
+    """Mirror of ``pp_tiling``."""
+
+    _fields_ = [
+        ("ntiles", _i32), ("halo_cap", _i32),
+        ("perm", _vp), ("inv", _vp), ("tile_start", _vp), ("halo", _vp),
+        ("halo_count", _vp), ("own_off", _vp), ("row_off", _vp),
+        ("entry", _vp), ("slot", _vp), ("bond_type", _vp), ("regime", _vp),
+        ("correction", _vp), ("r0", _vp), ("bc_values", _vp),
+        ("fc_values", _vp), ("node_instance", _vp), ("n_neigh", _vp),
+        ("sched", _vp),
     ]
 
 
@@ -171,6 +189,14 @@ SIGNATURES = {
     "pp_fused_run_static": (
         ctypes.c_int, [ctypes.POINTER(FusedArgs), _i32, _i64, _vp, _vp, _vp]),
     "pp_static_status": (ctypes.c_int, [_vp, _vp]),
+    "pp_cy_check_symmetric": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp,
+                                             _vp]),
+    "pp_tile_halos": (ctypes.c_int, [ctypes.POINTER(FusedArgs),
+                                     ctypes.POINTER(Tiling), _vp]),
+    "pp_tile_rows": (ctypes.c_int, [ctypes.POINTER(FusedArgs),
+                                    ctypes.POINTER(Tiling), _vp]),
+    "pp_host_register": (ctypes.c_int, [_vp, ctypes.c_size_t]),
+    "pp_host_unregister": (ctypes.c_int, [_vp]),
 }
 
 _lock = threading.Lock()

@@ -42,9 +42,10 @@ def tune_mixed(integ, warmup=3, reps=10):
     """
     import torch
     fa = integ._fargs
+    tiling = getattr(integ, "tiling", None)
     key = ("mixed", fa.nnodes, fa.max_neigh, fa.integrator,
            bool(fa.stiffness_corrections), bool(fa.bond_types),
-           bool(fa.node_instance), fa.flags)
+           bool(fa.node_instance), fa.flags, tiling is not None)
     if key in _cache:
         fa.variant = _cache[key][0]
         return _cache[key][1]
@@ -70,6 +71,17 @@ def tune_mixed(integ, warmup=3, reps=10):
         for k in range(2):
             scratch.rec[k] = clone(scratch.rec[k], integ.rec_d[k])
             scratch.ulo[k] = clone(scratch.ulo[k], integ.ulo_d[k])
+        if tiling is not None:
+            # the tiled step writes entries (breaks), regimes, the intact
+            # counts and the scheduler words of its tiling
+            st = _lib.Tiling()
+            ctypes.pointer(st)[0] = tiling.struct
+            st.entry = clone(st.entry, tiling.entry_d)
+            st.regime = clone(st.regime, tiling.regime_d)
+            st.n_neigh = clone(st.n_neigh, tiling.n_neigh_d)
+            st.sched = clone(st.sched, tiling.sched_d)
+            keep.append(st)
+            scratch.tiling = ctypes.addressof(st)
         results = {}
         stream = integ.context.stream
         for variant in range(_lib.PP_MIXED_VARIANTS):

@@ -25,8 +25,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE)]
 #: Per-unit flags.  The mixed-precision step accepts flushed denormals and
 #: approximate FP32 division/square root: its error band covers them.
-UNIT_FLAGS = {"pp_mixed": ["-ftz=true", "-prec-div=false",
-                           "-prec-sqrt=false"]}
+_FAST_FP32 = ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
+UNIT_FLAGS = {"pp_mixed": _FAST_FP32, "pp_tiled": _FAST_FP32}
 
 
 def _nvcc():

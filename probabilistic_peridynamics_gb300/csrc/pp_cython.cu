@@ -426,6 +426,37 @@ __global__ void k_cy_damage(const int32_t* __restrict__ n_neigh, const int32_t* 
     damage[i] = ddiv(dsub(f, (double)n_neigh[i]), f);
 }
 
+// Symmetry of compact rows: every entry j of row i (first n_neigh[i]
+// entries, width `w`) must be a node whose row holds i exactly as often as
+// row i holds j.  One warp per row; lane l takes entries l, l + 32, ... and
+// counts both multiplicities by scanning the two rows.  *bad counts the
+// entries that fail (out of range, or unequal multiplicities).
+__global__ void k_cy_symmetric(const int32_t* __restrict__ nlist,
+                               const int32_t* __restrict__ n_neigh, int nnodes, int w,
+                               unsigned int* __restrict__ bad) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= nnodes) return;
+    const int ni = min(max(n_neigh[i], 0), w);
+    const int32_t* ri = nlist + (int64_t)i * w;
+    unsigned int nbad = 0;
+    for (int k = lane; k < ni; k += 32) {
+        const int j = ri[k];
+        if (j < 0 || j >= nnodes) {
+            ++nbad;
+            continue;
+        }
+        const int nj = min(max(n_neigh[j], 0), w);
+        const int32_t* rj = nlist + (int64_t)j * w;
+        int fwd = 0, back = 0;
+        for (int t = 0; t < ni; ++t) fwd += ri[t] == j;
+        for (int t = 0; t < nj; ++t) back += rj[t] == i;
+        nbad += fwd != back;
+    }
+    nbad = __reduce_add_sync(kFull, nbad);
+    if (lane == 0 && nbad) atomicAdd(bad, nbad);
+}
+
 constexpr int kBreakWarps = 4;
 
 int warps_for(size_t per_warp) {
@@ -566,6 +597,18 @@ extern "C" int pp_cy_update_displacement(double* u, const double* bc_values,
     const int64_t ndof = 3 * (int64_t)nnodes;
     k_cy_update<<<(unsigned)((ndof + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         u, bc_values, bc_types, force, bc_scale, dt, ndof);
+    return launch_status();
+}
+
+extern "C" int pp_cy_check_symmetric(const int32_t* nlist, const int32_t* n_neigh,
+                                     int32_t nnodes, int32_t width, uint32_t* bad,
+                                     void* stream) {
+    if (nnodes < 0 || width < 0 || width > 1024 || !bad) return PP_ERROR_INVALID_VALUE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(bad, 0, sizeof(uint32_t), st) != cudaSuccess) return PP_ERROR_CUDA;
+    if (nnodes == 0 || width == 0) return PP_SUCCESS;
+    if (!nlist || !n_neigh) return PP_ERROR_INVALID_VALUE;
+    k_cy_symmetric<<<(nnodes + 7) / 8, 256, 0, st>>>(nlist, n_neigh, nnodes, width, bad);
     return launch_status();
 }
 

@@ -1,23 +1,30 @@
 // pp_mixed.cu -- PP_MIXED set-up (pack, export, bond extent), argument
 // checks and dispatch of a step to its tile shape.  The kernel itself is in
 // pp_mixed.cuh, instantiated per tile shape in pp_mixed_v*.cu.
-#include "pp_mixed.cuh"
+#include "pp_tiled.cuh"
 
 namespace pp {
+namespace tiling {
+int tile_export(const pp_fused_args& a, cudaStream_t st);
+int validate_tiling(const pp_fused_args& a);
+}  // namespace tiling
+
 namespace mixed {
 namespace {
 
 // ------------------------------------------------------ pack / export
-__global__ void k_mixed_pack(pp_fused_args a, int parity) {
+// Node i of the mixed layout from reference node perm[i] (perm NULL: i).
+__global__ void k_mixed_pack(pp_fused_args a, int parity, const int32_t* __restrict__ perm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.nnodes) return;
-    const int64_t o = 3 * (int64_t)i;
+    const int64_t src = perm ? perm[i] : i;
+    const int64_t o = 3 * src;
     int4 q;
     const double inv = 1.0 / a.pos_scale;  // pos_scale is a power of two: exact
     q.x = (int)llrint((a.r0[o] - a.pos_origin[0]) * inv);
     q.y = (int)llrint((a.r0[o + 1] - a.pos_origin[1]) * inv);
     q.z = (int)llrint((a.r0[o + 2] - a.pos_origin[2]) * inv);
-    const double w = a.bond_types ? a.vols[i] : a.bond_stiffness * a.vols[i];
+    const double w = a.bond_types ? a.vols[src] : a.bond_stiffness * a.vols[src];
     q.w = __float_as_int((float)w);
     float* rec = a.rec[parity] + 8 * (int64_t)i;
     reinterpret_cast<int4*>(rec)[0] = q;
@@ -49,17 +56,21 @@ __global__ void k_mixed_pack(pp_fused_args a, int parity) {
         a.acc[4 * (int64_t)i + 3] = 0.f;
         a.rho32[4 * (int64_t)i + 3] = 1.f;
     }
-    if (a.sc32) {
+    if (a.sc32 && !perm) {
         const int64_t row = (int64_t)i * a.max_neigh;
         for (int k = 0; k < a.max_neigh; ++k)
             a.sc32[row + k] = (float)a.stiffness_corrections[row + k];
     }
 }
 
-__global__ void k_mixed_export(pp_fused_args a, int parity) {
+// Reference node perm[i] (perm NULL: i) from node i of the mixed layout;
+// with a tiling, n_neigh and damage from the tiling's intact counts.
+__global__ void k_mixed_export(pp_fused_args a, int parity, const int32_t* __restrict__ perm,
+                               const int32_t* __restrict__ tile_n_neigh) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.nnodes) return;
-    const int64_t o = 3 * (int64_t)i;
+    const int64_t dst = perm ? perm[i] : i;
+    const int64_t o = 3 * dst;
     for (int d = 0; d < 3; ++d) {
         a.u[parity][o + d] =
             df_to_double(df{a.rec[parity][8 * (int64_t)i + 4 + d], a.ulo[parity][4 * (int64_t)i + d]});
@@ -70,7 +81,12 @@ __global__ void k_mixed_export(pp_fused_args a, int parity) {
         if (a.force) a.force[o + d] = (double)a.frc[8 * (int64_t)i + d];
         if (a.body_force) a.body_force[o + d] = (double)a.frc[8 * (int64_t)i + 4 + d];
     }
-    if (a.damage) a.damage[i] = damage_of(a.n_neigh[i], a.family[i]);
+    if (tile_n_neigh) {
+        a.n_neigh[dst] = tile_n_neigh[i];
+        if (a.damage) a.damage[dst] = damage_of(tile_n_neigh[i], a.family[dst]);
+    } else if (a.damage) {
+        a.damage[i] = damage_of(a.n_neigh[i], a.family[i]);
+    }
 }
 
 __global__ void k_init_extent(unsigned long long* p) {
@@ -118,7 +134,12 @@ int validate_mixed(const pp_fused_args& a) {
         !aligned16(a.ulo[1]) || !aligned16(a.frc))
         return PP_ERROR_MISALIGNED;
     if (a.integrator != PP_EULER && (!a.vel || !a.acc || !a.rho32)) return PP_ERROR_INVALID_VALUE;
-    if (a.stiffness_corrections && !a.sc32) return PP_ERROR_INVALID_VALUE;
+    if (a.tiling) {
+        const int rc = tiling::validate_tiling(a);
+        if (rc != PP_SUCCESS) return rc;
+    } else if (a.stiffness_corrections && !a.sc32) {
+        return PP_ERROR_INVALID_VALUE;
+    }
     if (a.bond_types && a.nbond_types * a.nregimes > kMaxTable) return PP_ERROR_UNSUPPORTED;
     if (!(a.pos_scale > 0.0)) return PP_ERROR_INVALID_VALUE;
     if (a.variant < 0 || a.variant >= PP_MIXED_VARIANTS) return PP_ERROR_INVALID_VALUE;
@@ -129,6 +150,23 @@ int validate_mixed(const pp_fused_args& a) {
 }
 
 int launch_mixed_step(const pp_fused_args& a, int parity, const Launch& l, cudaStream_t st) {
+    if (a.tiling) {
+        // the node arrays the step reads by node, in internal order
+        const pp_tiling& t = *a.tiling;
+        pp_fused_args ai = a;
+        ai.r0 = t.r0;
+        ai.bc_values = t.bc_values;
+        ai.fc_values = t.fc_values;
+        ai.n_neigh = t.n_neigh;
+        ai.node_instance = t.node_instance;
+        ai.tiling = nullptr;
+        switch (a.variant) {
+            case 0: return tiled::launch_tiled_shape0(ai, t, parity, l, st);
+            case 1: return tiled::launch_tiled_shape1(ai, t, parity, l, st);
+            case 2: return tiled::launch_tiled_shape2(ai, t, parity, l, st);
+        }
+        return PP_ERROR_INVALID_VALUE;
+    }
     switch (a.variant) {
         case 0: return mixed::launch_mixed_shape0(a, parity, l, st);
         case 1: return mixed::launch_mixed_shape1(a, parity, l, st);
@@ -168,7 +206,9 @@ extern "C" int pp_mixed_pack(const pp_fused_args* args, int32_t parity, void* st
     if (!aligned32(a.rec[parity]) || !aligned16(a.ulo[parity])) return PP_ERROR_MISALIGNED;
     if (a.vel && (!a.acc || !a.rho32)) return PP_ERROR_INVALID_VALUE;
     if (a.sc32 && !a.stiffness_corrections) return PP_ERROR_INVALID_VALUE;
-    k_mixed_pack<<<(a.nnodes + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, parity);
+    if (a.tiling && !a.tiling->perm) return PP_ERROR_INVALID_VALUE;
+    k_mixed_pack<<<(a.nnodes + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        a, parity, a.tiling ? a.tiling->perm : nullptr);
     return launch_status();
 }
 
@@ -179,7 +219,11 @@ extern "C" int pp_mixed_export(const pp_fused_args* args, int32_t parity, void* 
     if (a.nnodes == 0) return PP_SUCCESS;
     if (!a.u[parity] || !a.rec[parity] || !a.ulo[parity] || !a.frc || !a.n_neigh || !a.family)
         return PP_ERROR_INVALID_VALUE;
-    k_mixed_export<<<(a.nnodes + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(a,
-                                                                                       parity);
-    return launch_status();
+    if (a.tiling && (!a.tiling->perm || !a.tiling->n_neigh)) return PP_ERROR_INVALID_VALUE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    k_mixed_export<<<(a.nnodes + 255) / 256, 256, 0, st>>>(
+        a, parity, a.tiling ? a.tiling->perm : nullptr, a.tiling ? a.tiling->n_neigh : nullptr);
+    const int rc = launch_status();
+    if (rc != PP_SUCCESS || !a.tiling) return rc;
+    return tiling::tile_export(a, st);
 }

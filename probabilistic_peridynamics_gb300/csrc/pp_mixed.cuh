@@ -679,14 +679,15 @@ __device__ __forceinline__ void bond_phase_group(const pp_fused_args& a, const M
         reinterpret_cast<float*>(&sh.frc[li])[sub >> 1] = v;
 }
 
-// Node phase of one chunk: thread (node, component) updates one DOF.
+// Node phase of one chunk: thread (node, component) updates one DOF of
+// node node0 + li; nodes at iend and beyond only join the warp's shuffles.
 template <class Shared>
 __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedConst& c,
                                            const Shared& sh, const StepMags& m, int parity,
-                                           int node0, int li) {
+                                           int node0, int li, int iend) {
     const int comp = threadIdx.x & 3;
     const int i = node0 + li;
-    const bool active = i < a.nnodes;
+    const bool active = i < iend;
     const float4 fr = sh.frc[li];
     const int64_t o4 = 4 * (int64_t)i + comp;
     const int64_t o3 = 3 * (int64_t)i + comp;
@@ -827,7 +828,7 @@ __global__ void __launch_bounds__(W * 32, MINB)
             }
             __syncthreads();
             for (int li = threadIdx.x >> 2; li < kChunk; li += blockDim.x >> 2)
-                node_phase(a, c, sh, m, parity, node0, li);
+                node_phase(a, c, sh, m, parity, node0, li, a.nnodes);
             __syncthreads();
         }
         return;
@@ -857,7 +858,7 @@ __global__ void __launch_bounds__(W * 32, MINB)
         }
         __syncthreads();
         for (int li = threadIdx.x >> 2; li < kChunk; li += blockDim.x >> 2)
-            node_phase(a, c, sh, m, parity, node0, li);
+            node_phase(a, c, sh, m, parity, node0, li, a.nnodes);
         __syncthreads();
     }
 }

@@ -5,10 +5,14 @@
 // of the boundary-condition magnitude schedule, and, for the mixed step,
 // the running max |u| and the status word -- lives in one file-scope
 // __device__ array, loaded with the library and kept until exit.  Its
-// device address is looked up once per device (cudaGetSymbolAddress, with
-// that device current) by the first call on that device.  All calls share
-// the array and leave their contents in it; calls whose work overlaps on
-// the GPU race on it.
+// device address is looked up (cudaGetSymbolAddress, with the device
+// current) by the first call in each CUDA context: the address is cached
+// per device together with the context's unique ID (cuCtxGetId), so a
+// device reset or a re-created primary context makes the next call look it
+// up again.  All calls share the array and leave their contents in it;
+// calls whose work overlaps on the GPU race on it.
+#include <cuda.h>  // CUcontext, CUresult (the driver calls go through entry points)
+
 #include <mutex>
 
 #include "pp_fused.cuh"
@@ -25,21 +29,63 @@ struct StaticScratch {
 __device__ __align__(256) StaticScratch g_static_scratch;
 
 constexpr int kMaxDevices = 64;
-StaticScratch* g_scratch_addr[kMaxDevices] = {};
+struct CachedAddress {
+    unsigned long long ctx_id;  // cuCtxGetId of the context it belongs to
+    StaticScratch* addr;
+};
+CachedAddress g_scratch_addr[kMaxDevices] = {};
 std::mutex g_scratch_mutex;
 
-// Device address of g_static_scratch on the current device (looked up once).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique ID of the current context (0 when there is none yet).
+int current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void* f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+    });
+    if (!get_current || !get_id) return PP_ERROR_CUDA;
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS) return PP_ERROR_CUDA;
+    *id = 0;
+    if (ctx && get_id(ctx, id) != CUDA_SUCCESS) return PP_ERROR_CUDA;
+    return PP_SUCCESS;
+}
+
+// Device address of g_static_scratch in the current context (looked up by
+// the first call in each context).
 int scratch_address(StaticScratch** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return PP_ERROR_CUDA;
     if (dev < 0 || dev >= kMaxDevices) return PP_ERROR_UNSUPPORTED;
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
+    unsigned long long id = 0;
+    int rc = current_context_id(&id);
+    if (rc != PP_SUCCESS) return rc;
+    CachedAddress& c = g_scratch_addr[dev];
+    if (id == 0 || !c.addr || c.ctx_id != id) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p) return PP_ERROR_CUDA;
-        g_scratch_addr[dev] = static_cast<StaticScratch*>(p);
+        // the lookup makes the primary context current if none was
+        rc = current_context_id(&id);
+        if (rc != PP_SUCCESS || id == 0) return PP_ERROR_CUDA;
+        c.addr = static_cast<StaticScratch*>(p);
+        c.ctx_id = id;
     }
-    *out = g_scratch_addr[dev];
+    *out = c.addr;
     return PP_SUCCESS;
 }
 

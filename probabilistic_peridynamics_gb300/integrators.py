@@ -173,7 +173,7 @@ class _CUDAIntegrator(Integrator):
 
     def __init__(self, dt, context=None, fused=True, precision="float64",
                  compensated=False, nodes_per_block=0, use_graph=True,
-                 autotune=True):
+                 autotune=True, tiled=True):
         super().__init__(dt, context)
         if precision not in ("float64", "mixed"):
             raise ValueError("precision must be 'float64' or 'mixed' "
@@ -190,6 +190,11 @@ class _CUDAIntegrator(Integrator):
         self.nodes_per_block = int(nodes_per_block)
         self.use_graph = bool(use_graph)
         self.autotune = bool(autotune)
+        # mixed precision: gather neighbour records from shared memory on
+        # the tiled layout (False: the untiled kernel, from L1/L2)
+        self.tiled = bool(tiled) and precision == "mixed"
+        self.tiling = None
+        self._order = None
         self.tuning = None
         self.damping = 0.0
         self._parity = 0
@@ -292,6 +297,11 @@ class _CUDAIntegrator(Integrator):
             raise ValueError("bond_types shape must be (nnodes, "
                              "max_neighbours)")
         self._torch = torch
+        if self.tiled:
+            from .tiling import brick_order
+            self._order = brick_order(
+                self.coords, None if self._instances is None
+                else self._instances[0])
         self._build_special()
 
     def _check_densities(self):
@@ -406,6 +416,15 @@ class _CUDAIntegrator(Integrator):
                 _ptr(self.bond_length_d), self._stream), "pp_bond_lengths")
         self._fargs = self._make_fused_args() if self.fused else None
         if self.precision == "mixed":
+            if self.tiled:
+                from .tiling import DeviceTiling
+                self.tiling = DeviceTiling(*self._order, self.context.device)
+                self.tiling.build(
+                    self._fargs, self._stream,
+                    corrections=self.stiffness_corrections_d is not None,
+                    types=self.bond_types_d is not None,
+                    instances=self.node_instance_d is not None)
+                self._fargs.tiling = ctypes.addressof(self.tiling.struct)
             check(lib().pp_mixed_pack(ctypes.byref(self._fargs), 0,
                                       self._stream), "pp_mixed_pack")
             if self.autotune:
@@ -427,6 +446,7 @@ class _CUDAIntegrator(Integrator):
         else:
             self.vel_d = self.acc_d = self.rho32_d = None
         self.sc32_d = (None if self.stiffness_corrections_d is None
+                       or self.tiled
                        else self._empty((n, mn), torch.float32))
         self.nflags_d = self._empty((n,), torch.int32)
         self.umax_d = self._zeros((1,), torch.float32)
@@ -650,17 +670,19 @@ class _CUDAIntegrator(Integrator):
             # pages); if it cannot be registered it is copied as it is.
             # Memory that is pinned already (a view of a pinned tensor) is
             # left as it is: registering it again would fail.
+            # The registration goes through the library, whose own CUDA
+            # runtime keeps (and clears) the error of a failed attempt,
+            # e.g. when only part of the array is registered already.
             target = torch.from_numpy(host.reshape(-1))
             registered = False
             if host.nbytes >= _REGISTER_BYTES and not target.is_pinned():
-                cudart = torch.cuda.cudart()
-                registered = int(cudart.cudaHostRegister(
-                    host.ctypes.data, host.nbytes, 0)) == 0
+                registered = lib().pp_host_register(
+                    host.ctypes.data, host.nbytes) == _lib.PP_SUCCESS
             try:
                 target.copy_(dev.reshape(-1))
             finally:
                 if registered:
-                    cudart.cudaHostUnregister(host.ctypes.data)
+                    lib().pp_host_unregister(host.ctypes.data)
             return host
         src = dev.cpu().numpy()
         flat = host.reshape(-1)
@@ -822,14 +844,15 @@ class Euler(Integrator):
                              f"{width})")
         self._width = width
         with self.device_context.on_stream():
-            self._nlist_d = self._dev(nlist, np.int32, (n, width))
-            self._n_neigh_d = self._dev(n_neigh, np.int32, (n,))
-            if not self._symmetric():
+            nlist_d = self._dev(nlist, np.int32, (n, width))
+            n_neigh_d = self._dev(n_neigh, np.int32, (n,))
+            if not self._symmetric(nlist_d, n_neigh_d, width):
                 raise ValueError(
                     "the GPU Euler integrator needs a symmetric neighbour "
                     "list (j among the first n_neigh[i] entries of row i "
                     "exactly when i is among those of row j), as Model "
                     "builds it; this list is not")
+            self._nlist_d, self._n_neigh_d = nlist_d, n_neigh_d
             self._u_d = self._dev(u, np.float64, (n, 3))
             self._force_d = self._dev(force, np.float64, (n, 3))
             self._damage_d = torch.empty(n, dtype=torch.float64,
@@ -845,23 +868,16 @@ class Euler(Integrator):
                     _ptr(self._l0_d), self.device_context.stream_handle),
                     "pp_bond_lengths")
 
-    def _symmetric(self):
-        """Is j a valid entry of row i exactly when i is one of row j?
-        (Compares the sorted pairs (i, j) with the sorted pairs (j, i).)"""
+    def _symmetric(self, nlist_d, n_neigh_d, width):
+        """Is j an entry of row i exactly as often as i is one of row j?
+        (``pp_cy_check_symmetric``: one warp per row on the device.)"""
         import torch
-        n, w = self.nnodes, self._width
-        if n == 0 or w == 0:
-            return True
-        dev = self.device_context.device
-        counts = self._n_neigh_d.clamp(0, w)
-        valid = (torch.arange(w, device=dev)[None, :] < counts[:, None])
-        j = self._nlist_d[valid].long()
-        if bool(((j < 0) | (j >= n)).any()):
-            return False
-        i = torch.arange(n, device=dev)[:, None].expand(n, w)[valid].long()
-        forward = torch.sort(i * n + j).values
-        backward = torch.sort(j * n + i).values
-        return bool(torch.equal(forward, backward))
+        bad = torch.empty(1, dtype=torch.int32,
+                          device=self.device_context.device)
+        check(lib().pp_cy_check_symmetric(
+            _ptr(nlist_d), _ptr(n_neigh_d), self.nnodes, width, _ptr(bad),
+            self.device_context.stream_handle), "pp_cy_check_symmetric")
+        return int(bad.cpu().item()) == 0
 
     def __call__(self, displacement_bc_magnitude, force_bc_magnitude):
         """One step: break bonds, bond forces, Euler update

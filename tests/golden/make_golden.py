@@ -1,9 +1,10 @@
 """Build the golden fixtures in this directory from the reference's test data.
 
-Run in a container that has the reference checkout (read-only) at
-``/root/reference``::
+Run where the reference checkout (read-only) is available: its directory is
+the first argument, else ``$PP_REFERENCE``, else ``reference`` beside this
+repository's checkout::
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py [path/to/reference]
 
 It reads the regression inputs and expected outputs that the reference's own
 tests load (``peripy/test/data``, used by ``peripy/test/test_integrators.py``
@@ -24,6 +25,7 @@ Outputs:
                    (``test_integrators.py:150-195``).
 ``force3.npz``     the three-node mesh of the force test.
 """
+import os
 import pathlib
 import sys
 
@@ -77,4 +79,6 @@ def main(reference_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    default = (os.environ.get("PP_REFERENCE")
+               or HERE.parent.parent.parent / "reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else default)

@@ -43,7 +43,7 @@ def test_header_functions_exported(L):
 
 
 def test_abi_version_and_status_strings(L):
-    assert L.pp_abi_version() == 2
+    assert L.pp_abi_version() == 3
     assert L.pp_status_string(0) == b"success"
     assert b"power of two" in L.pp_status_string(2)
 
@@ -60,7 +60,50 @@ def test_struct_layout_matches_header():
     assert f["dt"].offset == 40
     assert f["bond_stiffness_table"].offset == 72
     assert f["bond_length"].offset == f["bond_types"].offset + 8
-    assert f["pos_origin"].offset + 24 == ctypes.sizeof(_lib.FusedArgs)
+    assert f["pos_origin"].offset + 24 == f["tiling"].offset
+    assert f["tiling"].offset + 8 == ctypes.sizeof(_lib.FusedArgs)
+    # pp_tiling: 2 int32 then 18 pointers
+    assert ctypes.sizeof(_lib.Tiling) == 2 * 4 + 18 * 8
+    assert _lib.Tiling.perm.offset == 8
+    assert _lib.Tiling.sched.offset == 8 + 17 * 8
+
+
+def test_struct_layout_matches_c_compiler(tmp_path):
+    """sizeof and offsetof of the C structs, compiled from the header with
+    the host C compiler, equal the ctypes mirrors."""
+    import shutil
+    import subprocess
+    from probabilistic_peridynamics_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    checks = {"pp_fused_args": (_lib.FusedArgs, ("variant", "dt", "nlist",
+                                                "rec", "pos_origin",
+                                                "tiling")),
+              "pp_tiling": (_lib.Tiling, ("perm", "entry", "correction",
+                                          "n_neigh", "sched")),
+              "pp_corrections_args": (_lib.CorrectionsArgs, ("r0",)),
+              "pp_write_sums_args": (_lib.WriteSumsArgs, ("u", "sums")),
+              "pp_adjoint_args": (_lib.AdjointArgs, ("r0", "stiffness"))}
+    lines = ['#include <stdio.h>', '#include <stddef.h>',
+             f'#include "{HEADER}"', "int main(void) {"]
+    for struct, (_, fields) in checks.items():
+        lines.append(f'printf("{struct} %zu\\n", sizeof({struct}));')
+        for f in fields:
+            lines.append(f'printf("{struct}.{f} %zu\\n", '
+                         f'offsetof({struct}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run(
+        [str(exe)], check=True, capture_output=True,
+        text=True).stdout.splitlines())
+    for struct, (cls, fields) in checks.items():
+        assert int(out[struct]) == ctypes.sizeof(cls), struct
+        for f in fields:
+            assert int(out[f"{struct}.{f}"]) == getattr(cls, f).offset, f
     # pp_corrections_args: 6 int32, 5 doubles, 6 pointers
     assert ctypes.sizeof(_lib.CorrectionsArgs) == 6 * 4 + 5 * 8 + 6 * 8
     assert _lib.CorrectionsArgs.r0.offset == 64

@@ -160,7 +160,8 @@ def test_write_into_registered_and_pinned_arrays(monkeypatch):
     """Integrator.write page-locks large host arrays for the copy (every
     array here, with the size threshold at 0) and leaves memory that is
     pinned already alone; the values are those of an ordinary copy and no
-    CUDA error is left behind."""
+    CUDA error is left behind, also when part of a target array was
+    registered beforehand, so that registering the whole array fails."""
     import torch
     import probabilistic_peridynamics_gb300 as pp
     from probabilistic_peridynamics_gb300 import integrators
@@ -168,7 +169,8 @@ def test_write_into_registered_and_pinned_arrays(monkeypatch):
     setup = breaking_setup("velocity_verlet")
     n = setup["nnodes"]
     outs = []
-    for mode in ("plain", "registered", "pinned"):
+    partial = None
+    for mode in ("plain", "registered", "pinned", "partly_registered"):
         monkeypatch.setattr(integrators, "_REGISTER_BYTES",
                             1 << 40 if mode == "plain" else 0)
         integ = pp.VelocityVerletCUDA(0.5, dt=setup["dt"])
@@ -193,8 +195,28 @@ def test_write_into_registered_and_pinned_arrays(monkeypatch):
         else:
             host = [np.zeros((n, 3)) for _ in range(5)]
             nl = np.zeros_like(setup["nlist"])
-        out = integ.write(*host, np.zeros(n), nl,
-                          np.zeros(n, dtype=np.intc))
+        if mode == "partly_registered":
+            # whole pages inside the neighbour-list target are registered
+            # beforehand: registering the whole array then fails
+            # (cudaErrorHostMemoryAlreadyRegistered), the copy goes ahead
+            # unregistered and no error may reach torch's next launch
+            page = 4096
+            lo = -(-nl.ctypes.data // page) * page
+            hi = (nl.ctypes.data + nl.nbytes) // page * page
+            assert hi > lo
+            cudart = torch.cuda.cudart()
+            assert int(cudart.cudaHostRegister(lo, hi - lo, 0)) == 0
+            partial = lo
+        try:
+            out = integ.write(*host, np.zeros(n), nl,
+                              np.zeros(n, dtype=np.intc))
+            y = torch.ones(4, device="cuda") * 3  # a launch right after
+            torch.cuda.synchronize()
+            assert float(y.sum()) == 12.0
+        finally:
+            if partial is not None:
+                torch.cuda.cudart().cudaHostUnregister(partial)
+                partial = None
         outs.append([np.array(a, copy=True) for a in out])
     for other in outs[1:]:
         for a, b in zip(outs[0], other):

@@ -99,3 +99,40 @@ def test_static_run_rejects_too_many_steps():
                                integ._stream)
     assert rc == _lib.PP_ERROR_TOO_LARGE
     assert b"PP_STATIC_MAX_STEPS" in L.pp_status_string(rc)
+
+
+@pytest.mark.parametrize("precision", ["float64", "mixed"])
+def test_static_run_leaves_device_memory_unchanged(precision):
+    """Free device memory (cudaMemGetInfo) is the same before and after the
+    first ``pp_fused_run_static`` call and after a second one.
+
+    The CUDA runtime loads a library's module lazily, at its first use in a
+    context; that load places the module's code and its file-scope array
+    (the 1 MB schedule buffer) in device memory, where they stay until the
+    process exits.  ``pp_static_status`` is called first so that this load
+    happens before the measurement: what is measured is the call itself.
+    """
+    import torch
+    from probabilistic_peridynamics_gb300 import _lib
+    L = _lib.lib()
+    setup = _setup()
+    steps = 40
+    disp = np.ascontiguousarray(3e-3 * np.arange(1, 2 * steps + 1))
+    force = np.zeros(2 * steps)
+    ref = _integrator(setup, precision)
+    ref._run(disp, force, 0, steps)  # loads the step kernels' modules
+    integ = _integrator(setup, precision)
+    status = ctypes.c_int32(-1)
+    assert L.pp_static_status(ctypes.byref(status), integ._stream) == 0
+    torch.cuda.synchronize()
+    free = [torch.cuda.mem_get_info()[0]]
+    for first in (0, steps):
+        rc = L.pp_fused_run_static(
+            ctypes.byref(integ._fargs), integ._parity, steps,
+            disp[first:].ctypes.data_as(ctypes.c_void_p),
+            force[first:].ctypes.data_as(ctypes.c_void_p), integ._stream)
+        assert rc == _lib.PP_SUCCESS, L.pp_status_string(rc)
+        integ._parity ^= steps & 1
+        torch.cuda.synchronize()
+        free.append(torch.cuda.mem_get_info()[0])
+    assert free[1] == free[0] and free[2] == free[0], free
