@@ -111,9 +111,24 @@ def profile_case(which):
         return
     w = build_workload()
     precision = "mixed" if which == "mixed" else "float64"
-    integ = make_integrator(w, precision, which != "plain", autotune=False)
     if which == "mixed":
-        integ._fargs.variant = int(os.environ.get("PP_PROFILE_VARIANT", "1"))
+        # PP_PROFILE_TILED=0: the untiled kernel (k_mixed), else k_tiled
+        tiled = os.environ.get("PP_PROFILE_TILED", "1") != "0"
+        import probabilistic_peridynamics_gb300 as pp
+        integ = pp.VelocityVerletCUDA(DAMPING, dt=DT, precision="mixed",
+                                      autotune=False, tiled=tiled)
+        integ.build(w["nnodes"], 3, w["max_neigh"], w["coords"],
+                    w["volume"], w["family"], w["bc_types"], w["bc_values"],
+                    w["force_bc_types"], w["force_bc_values"], None, None,
+                    w["densities"])
+        z = np.zeros((w["nnodes"], 3))
+        integ.create_buffers(w["nlist"], w["n_neigh"], w["k"], w["s0"], None,
+                             z, z, z, z, z, np.zeros(w["nnodes"]), None, 1, 1)
+        integ._fargs.variant = int(os.environ.get(
+            "PP_PROFILE_VARIANT", "0" if tiled else "1"))
+    else:
+        integ = make_integrator(w, precision, which != "plain",
+                                autotune=False)
     for k in range(6):
         integ(PULL_RATE * (k + 1), 0.0)
     integ.context.stream.synchronize()
@@ -130,8 +145,10 @@ def profile_composite():
     from probabilistic_peridynamics_gb300.pointset import composite
     w = composite(context=CUDAContext(0))
     n = w["coords"].shape[0]
+    tiled = os.environ.get("PP_PROFILE_TILED", "1") != "0"
     integ = pp.VelocityVerletCUDA(DAMPING, dt=DT, precision="mixed",
-                                  compensated=True, autotune=False)
+                                  compensated=True, autotune=False,
+                                  tiled=tiled)
     integ.build(n, 3, w["max_neigh"], w["coords"], w["volume"], w["family"],
                 w["bc_types"], w["bc_values"], np.zeros((n, 3), dtype=np.intc),
                 np.zeros((n, 3)), None, w["bond_types"], w["densities"])

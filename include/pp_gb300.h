@@ -196,22 +196,28 @@ int pp_update_displacement_velocity_verlet(
 /* of a tile is the ascending list of internal nodes its bonds reach (its   */
 /* own nodes included), at most halo_cap long.  A step stages each tile's   */
 /* halo records in shared memory once and gathers every bond of the tile   */
-/* from there.  Row i holds the bonds of internal node i as 16-bit indices  */
-/* into its tile's halo ("entries"), 0xFFFF for broken bonds and padding,   */
-/* in the reference row's slot order, CSR-packed: row i occupies entries    */
+/* from there.  Row i holds the bonds of internal node i as 16-bit entries, */
+/* each 16 x the halo index of the neighbour (the byte offset of its staged */
+/* record); a broken bond or padding holds the entry of node i itself.     */
+/* Rows follow the reference row's slot order, CSR-packed: row i occupies   */
 /* [16 row_off[i], 16 row_off[i+1]), its length the number of its intact   */
 /* slots rounded up to 16.  Row entry p = 16 m + 8 h + l (l < 8, h < 2) is  */
 /* stored at position 16 m + 2 l + h of the row, so that lane l of a node's */
 /* eight lanes reads its entries 16 m + l and 16 m + 8 + l with one 32-bit  */
 /* load.  Any permutation and any cut into ranges gives the same results;   */
-/* spatial locality of the tiles only makes the step faster.                */
+/* spatial locality of the tiles only makes the step faster.  (A node      */
+/* listed as its own neighbour is held as a broken bond from the start;    */
+/* the reference breaks it in the first step, its stretch being 0/0.)      */
 /*                                                                          */
 /* The caller allocates every array and chooses perm and tile_start;       */
 /* pp_tile_halos and pp_tile_rows fill the rest from the reference layouts. */
+/* The step trusts the entries as it trusts a reference neighbour list:    */
+/* they must be those pp_tile_rows wrote, as the steps since have left them. */
 /* ------------------------------------------------------------------------ */
 
 #define PP_TILE_NODES_MAX           128   /* internal nodes per tile       */
-#define PP_TILE_HALO_MAX            4096  /* largest halo_cap              */
+#define PP_TILE_HALO_MAX            1536  /* largest halo_cap: 32 bytes of
+                                             shared memory per record      */
 
 typedef struct pp_tiling {
     int32_t ntiles;
@@ -223,8 +229,12 @@ typedef struct pp_tiling {
     int32_t* halo;             /* (ntiles * halo_cap) internal nodes       */
     int32_t* halo_count;       /* (ntiles) halo lengths (pp_tile_halos)    */
     int32_t* own_off;          /* (ntiles) halo index of the tile's first node */
+    int32_t* tile_ref;         /* (ntiles * 4) the tile's reference point in
+                                  fixed-point steps (x, y, z, 0): staged
+                                  positions are float(q - ref) * pos_scale,
+                                  exact because |q - ref| < 2^22          */
     int32_t* row_off;          /* (nnodes + 1) row offsets, units of 16 entries */
-    uint16_t* entry;           /* (16 row_off[nnodes]) halo index per entry */
+    uint16_t* entry;           /* (16 row_off[nnodes]) 16 x halo index     */
     uint8_t* slot;             /* same length: the entry's slot in the
                                   reference row, 0xFF for padding         */
     uint8_t* bond_type;        /* same length, or NULL without bond types  */
@@ -370,11 +380,13 @@ int pp_mixed_pack(const pp_fused_args* args, int32_t parity, void* stream);
 int pp_mixed_export(const pp_fused_args* args, int32_t parity, void* stream);
 
 /* Tiled layout, first part: from the reference nlist (args->nlist,
- * args->max_neigh) and t->perm, inv, tile_start, ntiles, halo_cap, writes
- * halo, halo_count, own_off and row_off.  A tile whose halo would exceed
- * halo_cap gets halo_count = its halo's length (> halo_cap) and no halo:
- * the caller splits it and calls again.  On return (after the stream),
- * row_off[nnodes] is the number of 16-entry blocks the rows need. */
+ * args->max_neigh), args->r0, pos_scale, pos_origin and t->perm, inv,
+ * tile_start, ntiles, halo_cap, writes halo, halo_count, own_off, tile_ref
+ * and row_off.  A tile whose halo would exceed halo_cap, or would reach
+ * 2^22 fixed-point steps or more from the tile's reference point, gets a
+ * halo_count above halo_cap and no halo: the caller splits it and calls
+ * again.  On return (after the stream), row_off[nnodes] is the number of
+ * 16-entry blocks the rows need. */
 int pp_tile_halos(const pp_fused_args* args, const pp_tiling* t, void* stream);
 
 /* Tiled layout, second part (every halo_count <= halo_cap): writes entry,

@@ -34,7 +34,7 @@ PP_STATUS_OK = 0
 PP_STATUS_COPY_TIMEOUT = 1
 PP_STATUS_BAD_TILING = 2
 PP_TILE_NODES_MAX = 128
-PP_TILE_HALO_MAX = 4096
+PP_TILE_HALO_MAX = 1536
 
 _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
@@ -93,7 +93,8 @@ class Tiling(ctypes.Structure):
     _fields_ = [
         ("ntiles", _i32), ("halo_cap", _i32),
         ("perm", _vp), ("inv", _vp), ("tile_start", _vp), ("halo", _vp),
-        ("halo_count", _vp), ("own_off", _vp), ("row_off", _vp),
+        ("halo_count", _vp), ("own_off", _vp), ("tile_ref", _vp),
+        ("row_off", _vp),
         ("entry", _vp), ("slot", _vp), ("bond_type", _vp), ("regime", _vp),
         ("correction", _vp), ("r0", _vp), ("bc_values", _vp),
         ("fc_values", _vp), ("node_instance", _vp), ("n_neigh", _vp),

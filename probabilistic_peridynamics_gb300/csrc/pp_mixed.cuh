@@ -107,11 +107,10 @@ __device__ __forceinline__ float fixed_diff(int qj, int qi, const MixedConst& c)
     return fmaf(__int_as_float(qj - qi + kMagicI), c.h, c.mh);
 }
 
-__device__ __forceinline__ Bond32 bond32(const int4& qi, const float4& ui, const int4& qj,
-                                         const float4& uj, const MixedConst& c) {
-    const float xx = fixed_diff(qj.x, qi.x, c);
-    const float xy = fixed_diff(qj.y, qi.y, c);
-    const float xz = fixed_diff(qj.z, qi.z, c);
+// FP32 quantities of a bond from its exact reference vector xi = (xx, xy,
+// xz) and the displacement halves of both ends.
+__device__ __forceinline__ Bond32 bond32_xi(float xx, float xy, float xz, const float4& ui,
+                                            const float4& uj) {
     const float ex = uj.x - ui.x, ey = uj.y - ui.y, ez = uj.z - ui.z;
     Bond32 b;
     b.px = xx + ex;
@@ -127,6 +126,13 @@ __device__ __forceinline__ Bond32 bond32(const int4& qi, const float4& ui, const
     // s = (|p| - |xi|)/|xi| without cancellation: (2 xi.e + e.e)/(|xi|(|p|+|xi|))
     b.s = __fdividef(num * b.rxi, lsum);
     return b;
+}
+
+// The same from the fixed-point positions: xi = h (q_j - q_i), exact.
+__device__ __forceinline__ Bond32 bond32(const int4& qi, const float4& ui, const int4& qj,
+                                         const float4& uj, const MixedConst& c) {
+    return bond32_xi(fixed_diff(qj.x, qi.x, c), fixed_diff(qj.y, qi.y, c),
+                     fixed_diff(qj.z, qi.z, c), ui, uj);
 }
 
 // Bound on |s - s64| for one bond: s64 is the binary64 stretch of the same

@@ -10,27 +10,31 @@
 //     last CTA to finish resets both counter words for the next launch:
 //     no CTA waits for another).
 //  1. Staging: the records of the tile's halo (every node its bonds reach,
-//     ascending) are copied from the state slot into shared memory with
-//     16-byte cp.async, as two arrays (positions + weight, displacements +
-//     max|u|) so that eight lanes reading eight consecutive records hit
-//     eight different bank quads.
+//     ascending) go to shared memory as two arrays, so that eight lanes
+//     reading eight consecutive records hit eight different bank quads:
+//     the displacement halves and max|u| by 16-byte cp.async, the
+//     positions converted to floats relative to the tile's reference point
+//     (exact: |q - ref| < 2^22 fixed-point steps) with the weight.  A bond
+//     vector is then one subtraction per component, exactly h (q_j - q_i).
 //  2. Bond phase: four nodes per warp, eight lanes per node; lane l reads
 //     its row entries 16 m + l and 16 m + 8 + l as one 32-bit word of two
-//     16-bit halo indices (the next two words are loaded while a batch of
-//     four computes), gathers both records from shared memory and does the
-//     FP32 bond arithmetic of bond32; a clearly intact bond is decided by
-//     one compare, every other one in the per-node slow path (own error
-//     band, else the binary64 stretch from the reference r0 and the exact
+//     16-bit entries (the next words are loaded while a batch computes),
+//     gathers both records from shared memory and does the FP32 bond
+//     arithmetic of bond32_xi; a clearly intact bond is decided by one
+//     compare, every other one in the per-node slow path (own error band,
+//     else the binary64 stretch from the reference r0 and the exact
 //     double-float displacement, peridynamics.cl:65-91).  A break writes
-//     0xFFFF into the entry.  The four per-node sums are reduced over the
+//     the node's own entry.  The four per-node sums are reduced over the
 //     eight lanes (4 shuffles) and parked in shared memory.
 //  3. Node phase: as k_mixed (double-float update, next records written
 //     with coalesced stores), for the tile's nodes.
 //
-// Every index read from the tiling is checked before it addresses shared
-// memory: a tile with more than PP_TILE_NODES_MAX nodes or a halo longer
-// than its capacity is skipped and reported in the status word
-// (PP_STATUS_BAD_TILING); an entry >= the halo length is a broken bond.
+// Entries are byte offsets (16 x halo index) into the staged arrays, so a
+// gather is one shared load at an immediate offset; a broken bond or
+// padding holds the node's own entry.  Every count read from the tiling is
+// checked before it addresses shared memory: a tile with more than
+// PP_TILE_NODES_MAX nodes or a halo longer than PP_TILE_HALO_MAX is
+// skipped and reported in the status word (PP_STATUS_BAD_TILING).
 #pragma once
 
 #include "pp_mixed.cuh"
@@ -41,6 +45,10 @@ namespace tiled {
 using namespace mixed;
 
 constexpr int kTileNodes = PP_TILE_NODES_MAX;
+constexpr int kHaloCap = PP_TILE_HALO_MAX;  // staged records per CTA
+// dynamic shared memory: positions at byte 0, displacements at kSuOffset
+constexpr int kSuOffset = 16 * kHaloCap;
+constexpr size_t kDynSmem = 32 * static_cast<size_t>(kHaloCap);
 
 struct Tables {
     float thr[kMaxTable], k[kMaxTable], c[kMaxTable];  // regime tables or
@@ -52,6 +60,11 @@ struct Tables {
 struct FrcView {
     const float4* frc;
 };
+
+// Staged record at byte offset `off` (an entry) of the array at `base`.
+__device__ __forceinline__ float4 staged(const unsigned char* base, int off) {
+    return *reinterpret_cast<const float4*>(base + off);
+}
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
@@ -75,23 +88,32 @@ __device__ __forceinline__ uint32_t load_u16x2(const uint8_t* p) {
 }
 
 // Bond phase of one node (eight lanes, lane `lane & 7` of them): internal
-// node n0 + li of tile `tile`, its record at halo index own0 + li.  Parks
-// (force x, y, z, intact count) in sfrc[li].  li >= nt: no node; the lanes
-// only join the warp's shuffles.
-template <bool CORR, bool TYPES, bool COMP>
+// node n0 + li of tile `tile`, its staged record at halo index own0 + li
+// (entry own0 + li times 16, which its broken bonds and padding hold).
+// Parks (force x, y, z, intact count) in sfrc[li].  li >= nt: no node; the
+// lanes only join the warp's shuffles.  NW: the most 32-bit entry words a
+// lane can have (max_neigh / 16); the loop over them is unrolled, so every
+// entry's bit and offset are constants, and stops at the warp's longest
+// row.  A batch takes G entries (G / 2 words).
+//
+// dsm: the staged positions relative to the tile's reference point
+// (float(q - ref) h, exact) with the weight, then (kSuOffset) the
+// displacement halves with max|u|.  The bond vector xj - xi is exactly
+// h (q_j - q_i), as in k_mixed.
+template <int NW, int G, bool CORR, bool TYPES, bool COMP>
 __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tiling& t,
                                           const MixedConst& c, const Thresholds& th0,
-                                          const Tables& tab, const int4* __restrict__ sq,
-                                          const float4* __restrict__ su,
+                                          const Tables& tab, const unsigned char* __restrict__ dsm,
                                           float4* __restrict__ sfrc, int parity, int tile,
-                                          int n0, int nt, int nh, int own0, int li, int lane) {
+                                          int n0, int nt, int own0, int li, int lane) {
+    constexpr int GW = G / 2;  // words per batch
     const int sub = lane & 7;
     const bool node_ok = li < nt;
     const int lic = node_ok ? li : 0;
     const int i = n0 + lic;
-    const int own = own0 + lic;
-    const int4 qi = sq[own];
-    const float4 ui = su[own];
+    const int self = 16 * (own0 + lic);  // this node's own entry
+    const float4 xi = staged(dsm, self);
+    const float4 ui = staged(dsm + kSuOffset, self);
     const int nr = a.nregimes;
     float s0f = c.s0, s0err = c.s0_err;
     double s0d = a.critical_stretch;
@@ -104,7 +126,7 @@ __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tilin
         th.lo = tab.tlo[inst];
         th.hi = tab.thi[inst];
     }
-    int np = 0;  // 32-bit words (pairs of entries) per lane
+    int np = 0;  // 32-bit words (pairs of entries) of this lane
     int64_t rowE = 0;
     if (node_ok) {
         const int r0 = t.row_off[i];
@@ -115,65 +137,76 @@ __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tilin
     // this lane's entry position of word m, half h: lp + 16 m + h
     const int64_t lp = rowE + 2 * sub;
     const uint32_t* ew = reinterpret_cast<const uint32_t*>(t.entry) + (lp >> 1);
+    const uint32_t none = static_cast<uint32_t>(self) * 0x10001u;  // two own entries
     float sx = 0.f, sy = 0.f, sz = 0.f;
     float cx = 0.f, cy = 0.f, cz = 0.f;  // carries (COMP)
     float cnt = 0.f;
     unsigned amb = 0u;
-    uint32_t wn0 = np > 0 ? load_word(ew) : 0xFFFFFFFFu;
-    uint32_t wn1 = np > 1 ? load_word(ew + 8) : 0xFFFFFFFFu;
-    for (int m0 = 0; m0 < npw; m0 += 2) {
-        const uint32_t w0 = wn0, w1 = wn1;
-        wn0 = m0 + 2 < np ? load_word(ew + 8 * (m0 + 2)) : 0xFFFFFFFFu;
-        wn1 = m0 + 3 < np ? load_word(ew + 8 * (m0 + 3)) : 0xFFFFFFFFu;
-        const int e[4] = {static_cast<int>(w0 & 0xFFFFu), static_cast<int>(w0 >> 16),
-                          static_cast<int>(w1 & 0xFFFFu), static_cast<int>(w1 >> 16)};
-        float sc[4];
-        int bt[4], rg[4];
-        if constexpr (CORR) {
-            const float2 z = make_float2(0.f, 0.f);
-            const float2 c0 =
-                m0 < np ? __ldcs(reinterpret_cast<const float2*>(t.correction + lp + 16 * m0)) : z;
-            const float2 c1 = m0 + 1 < np ? __ldcs(reinterpret_cast<const float2*>(
-                                                t.correction + lp + 16 * (m0 + 1)))
-                                          : z;
-            sc[0] = c0.x;
-            sc[1] = c0.y;
-            sc[2] = c1.x;
-            sc[3] = c1.y;
-        }
-        if constexpr (TYPES) {
-            const uint32_t b0 = m0 < np ? load_u16x2(t.bond_type + lp + 16 * m0) : 0u;
-            const uint32_t b1 = m0 + 1 < np ? load_u16x2(t.bond_type + lp + 16 * (m0 + 1)) : 0u;
-            const uint32_t g0 = m0 < np ? load_u16x2(t.regime + lp + 16 * m0) : 0u;
-            const uint32_t g1 = m0 + 1 < np ? load_u16x2(t.regime + lp + 16 * (m0 + 1)) : 0u;
-            bt[0] = (b0 & 0xFF) * nr;
-            bt[1] = (b0 >> 8) * nr;
-            bt[2] = (b1 & 0xFF) * nr;
-            bt[3] = (b1 >> 8) * nr;
-            rg[0] = g0 & 0xFF;
-            rg[1] = g0 >> 8;
-            rg[2] = g1 & 0xFF;
-            rg[3] = g1 >> 8;
-        }
-        int4 qj[4];
-        float4 uj[4];
+    uint32_t wn[GW];
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-            const int ee = e[kk] < nh ? e[kk] : own;
-            qj[kk] = sq[ee];
-            uj[kk] = su[ee];
+    for (int g = 0; g < GW; ++g) wn[g] = g < np ? load_word(ew + 8 * g) : none;
+#pragma unroll
+    for (int m0 = 0; m0 < NW; m0 += GW) {
+        if (m0 >= npw) break;  // warp-uniform
+        uint32_t w[GW];
+#pragma unroll
+        for (int g = 0; g < GW; ++g) {
+            w[g] = wn[g];
+            if (m0 + GW < NW) wn[g] = m0 + GW + g < np ? load_word(ew + 8 * (m0 + GW + g)) : none;
+        }
+        int e[G];
+#pragma unroll
+        for (int g = 0; g < GW; ++g) {
+            e[2 * g] = static_cast<int>(w[g] & 0xFFFFu);
+            e[2 * g + 1] = static_cast<int>(w[g] >> 16);
+        }
+        float sc[G];
+        int bt[G], rg[G];
+#pragma unroll
+        for (int g = 0; g < GW; ++g) {
+            const int m = m0 + g;
+            if constexpr (CORR) {
+                const float2 cv =
+                    m < np ? __ldcs(reinterpret_cast<const float2*>(t.correction + lp + 16 * m))
+                           : make_float2(0.f, 0.f);
+                sc[2 * g] = cv.x;
+                sc[2 * g + 1] = cv.y;
+            }
+            if constexpr (TYPES) {
+                const uint32_t bb = m < np ? load_u16x2(t.bond_type + lp + 16 * m) : 0u;
+                const uint32_t gg = m < np ? load_u16x2(t.regime + lp + 16 * m) : 0u;
+                bt[2 * g] = (bb & 0xFF) * nr;
+                bt[2 * g + 1] = (bb >> 8) * nr;
+                rg[2 * g] = gg & 0xFF;
+                rg[2 * g + 1] = gg >> 8;
+            }
+        }
+        float4 xj[G], uj[G];
+#pragma unroll
+        for (int kk = 0; kk < G; ++kk) {
+            xj[kk] = staged(dsm, e[kk]);
+            uj[kk] = staged(dsm + kSuOffset, e[kk]);
         }
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
+        for (int kk = 0; kk < G; ++kk) {
             const int k = 2 * m0 + kk;  // word k >> 1, half k & 1
-            const bool valid = e[kk] < nh;
-            const Bond32 b = bond32(qi, ui, qj[kk], uj[kk], c);
-            float w = __int_as_float(qj[kk].w);  // k*vol (PMB) or vol (types)
-            bool intact;
+            const bool valid = e[kk] != self;
+            const Bond32 b =
+                bond32_xi(xj[kk].x - xi.x, xj[kk].y - xi.y, xj[kk].z - xi.z, ui, uj[kk]);
+            float wt = xj[kk].w;  // k*vol (PMB) or vol (types)
             if constexpr (!TYPES) {
-                intact = valid && b.s < th.lo;
+                // clearly intact below th.lo; every other bond is decided in
+                // the slow path below, where breaks are written
+                const bool intact = valid && b.s < th.lo;
                 if (valid && !intact) amb |= 1u << k;
-                w *= b.s;
+                if (intact) {
+                    float fv = (wt * b.s) * b.ry;
+                    if constexpr (CORR) fv *= sc[kk];
+                    acc_mul<COMP>(sx, cx, fv, b.px);
+                    acc_mul<COMP>(sy, cy, fv, b.py);
+                    acc_mul<COMP>(sz, cz, fv, b.pz);
+                    cnt += 1.0f;
+                }
             } else {
                 if (!valid) continue;
                 bool ambiguous = false;
@@ -192,24 +225,23 @@ __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tilin
                 }
                 const int64_t pos = lp + 16 * (k >> 1) + (k & 1);
                 if (reg != rg[kk]) t.regime[pos] = static_cast<uint8_t>(reg);
-                intact = reg < nr;
-                if (!intact) {
-                    t.entry[pos] = 0xFFFF;
+                if (reg >= nr) {
+                    t.entry[pos] = static_cast<uint16_t>(self);
                     continue;
                 }
-                w *= fmaf(b.s, tab.k[bt[kk] + reg], tab.c[bt[kk] + reg]);
+                wt *= fmaf(b.s, tab.k[bt[kk] + reg], tab.c[bt[kk] + reg]);
+                float fv = wt * b.ry;
+                if constexpr (CORR) fv *= sc[kk];
+                acc_mul<COMP>(sx, cx, fv, b.px);
+                acc_mul<COMP>(sy, cy, fv, b.py);
+                acc_mul<COMP>(sz, cz, fv, b.pz);
+                cnt += 1.0f;
             }
-            float fv = intact ? w * b.ry : 0.0f;
-            if constexpr (CORR) fv *= sc[kk];
-            acc_mul<COMP>(sx, cx, fv, b.px);
-            acc_mul<COMP>(sy, cy, fv, b.py);
-            acc_mul<COMP>(sz, cz, fv, b.pz);
-            cnt += intact ? 1.0f : 0.0f;
         }
     }
     // Slow path: entries that break, or whose FP32 stretch is too close to
-    // a critical stretch.  Their halo index is read again; the records come
-    // from shared memory.
+    // a critical stretch.  Their entry is read again; the records come from
+    // shared memory.
     if (__any_sync(kFull, amb != 0u)) {
         const int32_t* hl = t.halo + (int64_t)tile * t.halo_cap;
 #pragma unroll 1
@@ -217,12 +249,13 @@ __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tilin
             const int k = __ffs(bits) - 1;
             const int64_t pos = lp + 16 * (k >> 1) + (k & 1);
             const int e = t.entry[pos];
-            if (e >= nh) continue;  // cannot happen: it was valid above
-            const int j = hl[e];
-            const int4 qj = sq[e];
-            const float4 uj = su[e];
-            const Bond32 b = bond32(qi, ui, qj, uj, c);
-            float w = __int_as_float(qj.w);
+            if (e == self) continue;  // cannot happen: it was valid above
+            const int j = hl[e >> 4];
+            if (static_cast<unsigned>(j) >= static_cast<unsigned>(a.nnodes)) continue;
+            const float4 xj = staged(dsm, e);
+            const float4 uj = staged(dsm + kSuOffset, e);
+            const Bond32 b = bond32_xi(xj.x - xi.x, xj.y - xi.y, xj.z - xi.z, ui, uj);
+            float wt = xj.w;
             bool intact;
             if constexpr (!TYPES) {
                 const float d = b.s - s0f;
@@ -232,7 +265,7 @@ __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tilin
                     intact = d < 0.0f;
                 else
                     intact = exact_stretch(a, parity, i, j) < s0d;
-                w *= b.s;
+                wt *= b.s;
             } else {
                 const double s64 = exact_stretch(a, parity, i, j);
                 const int btk = t.bond_type[pos] * nr;
@@ -242,13 +275,13 @@ __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tilin
                 });
                 if (reg != rgk) t.regime[pos] = static_cast<uint8_t>(reg);
                 intact = reg < nr;
-                if (intact) w *= fmaf(b.s, tab.k[btk + reg], tab.c[btk + reg]);
+                if (intact) wt *= fmaf(b.s, tab.k[btk + reg], tab.c[btk + reg]);
             }
             if (!intact) {
-                t.entry[pos] = 0xFFFF;
+                t.entry[pos] = static_cast<uint16_t>(self);
                 continue;
             }
-            float fv = w * b.ry;
+            float fv = wt * b.ry;
             if constexpr (CORR) fv *= t.correction[pos];
             acc_mul<COMP>(sx, cx, fv, b.px);
             acc_mul<COMP>(sy, cy, fv, b.py);
@@ -261,16 +294,19 @@ __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tilin
         v = reduce4c_group<8>(sx, cx, sy, cy, sz, cz, cnt, lane);
     else
         v = reduce4_group<8>(sx, sy, sz, cnt, lane);
-    if (node_ok && sub < 8 && (sub & 1) == 0) reinterpret_cast<float*>(&sfrc[li])[sub >> 1] = v;
+    if (node_ok && (sub & 1) == 0) reinterpret_cast<float*>(&sfrc[li])[sub >> 1] = v;
 }
 
 // One persistent CTA of W warps takes tiles until none are left.
-template <bool CORR, bool TYPES, bool COMP, int W, int MINB>
+template <int NW, bool CORR, bool TYPES, bool COMP, int W, int MINB>
 __global__ void __launch_bounds__(W * 32, MINB)
     k_tiled(pp_fused_args a, pp_tiling t, MixedConst c, int parity, Launch l) {
+    // entries per batch: 4; 2 with bond types, whose regime state and
+    // tables hold more registers per entry
+    constexpr int kG = TYPES ? 2 : 4;
     extern __shared__ __align__(16) unsigned char dsm[];
-    int4* sq = reinterpret_cast<int4*>(dsm);
-    float4* su = reinterpret_cast<float4*>(dsm + 16 * static_cast<size_t>(t.halo_cap));
+    float4* sp = reinterpret_cast<float4*>(dsm);
+    float4* su = reinterpret_cast<float4*>(dsm + kSuOffset);
     __shared__ __align__(16) float4 sfrc[kTileNodes];
     __shared__ Tables tab;
     __shared__ int s_tile;
@@ -310,22 +346,27 @@ __global__ void __launch_bounds__(W * 32, MINB)
         const int nt = t.tile_start[tile + 1] - n0;
         const int nh = t.halo_count[tile];
         const int own0 = t.own_off[tile];
-        const bool ok = nt >= 0 && nt <= kTileNodes && nh >= 0 && nh <= t.halo_cap &&
+        const bool ok = nt >= 0 && nt <= kTileNodes && nh >= 0 && nh <= kHaloCap &&
                         own0 >= 0 && own0 + nt <= nh && n0 >= 0 && n0 + nt <= a.nnodes;
         if (ok) {
             const int32_t* hl = t.halo + (int64_t)tile * t.halo_cap;
             const float* rec = a.rec[parity];
+            const int4 ref = reinterpret_cast<const int4*>(t.tile_ref)[tile];
+            // the displacement halves by cp.async; positions converted to
+            // floats relative to the tile's reference point on the way
             for (int h = threadIdx.x; h < nh; h += blockDim.x) {
                 int idx = hl[h];
                 idx = static_cast<unsigned>(idx) < static_cast<unsigned>(a.nnodes) ? idx : 0;
-                cp_async16(&sq[h], rec + 8 * (int64_t)idx);
                 cp_async16(&su[h], rec + 8 * (int64_t)idx + 4);
+                const int4 q = __ldg(reinterpret_cast<const int4*>(rec + 8 * (int64_t)idx));
+                sp[h] = make_float4(fixed_diff(q.x, ref.x, c), fixed_diff(q.y, ref.y, c),
+                                    fixed_diff(q.z, ref.z, c), __int_as_float(q.w));
             }
             cp_async_wait_all();
             __syncthreads();
             for (int base = warp * 4; base < nt; base += W * 4)  // warp-uniform
-                bond_tile<CORR, TYPES, COMP>(a, t, c, th0, tab, sq, su, sfrc, parity, tile, n0,
-                                             nt, nh, own0, base + (lane >> 3), lane);
+                bond_tile<NW, kG, CORR, TYPES, COMP>(a, t, c, th0, tab, dsm, sfrc, parity, tile,
+                                                     n0, nt, own0, base + (lane >> 3), lane);
             __syncthreads();
             for (int li = threadIdx.x >> 2; li < kTileNodes; li += blockDim.x >> 2)
                 node_phase(a, c, FrcView{sfrc}, m, parity, n0, li, n0 + nt);
@@ -348,49 +389,60 @@ __global__ void __launch_bounds__(W * 32, MINB)
     }
 }
 
-// Persistent launch: as many CTAs as fit on the device at once for this
-// halo capacity (cached per kernel instance and capacity).
-template <bool CORR, bool TYPES, bool COMP, int W, int MINB>
+// Persistent launch: as many CTAs as fit on the device at once (cached per
+// kernel instance).
+template <int NW, bool CORR, bool TYPES, bool COMP, int W, int MINB>
 int launch_tiled_instance(const pp_fused_args& a, const pp_tiling& t, int parity, const Launch& l,
                           cudaStream_t st) {
-    auto kernel = k_tiled<CORR, TYPES, COMP, W, MINB>;
-    static int cached_cap = -1, cached_grid = 0;
-    const size_t dyn = 32 * static_cast<size_t>(t.halo_cap);
-    if (cached_cap != t.halo_cap) {
+    auto kernel = k_tiled<NW, CORR, TYPES, COMP, W, MINB>;
+    static int cached_grid = 0;
+    if (cached_grid == 0) {
         if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(dyn)) != cudaSuccess)
+                                 static_cast<int>(kDynSmem)) != cudaSuccess)
             return PP_ERROR_CUDA;
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, W * 32, dyn) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, W * 32, kDynSmem) !=
                 cudaSuccess ||
             per_sm < 1)
-            return PP_ERROR_UNSUPPORTED;  // halo capacity too large for shared memory
+            return PP_ERROR_UNSUPPORTED;
         cached_grid = per_sm * sm_count();
-        cached_cap = t.halo_cap;
     }
     const int grid = t.ntiles < cached_grid ? t.ntiles : cached_grid;
     if (grid < 1) return PP_SUCCESS;
-    kernel<<<grid, W * 32, dyn, st>>>(a, t, mixed_const(a), parity, l);
+    kernel<<<grid, W * 32, kDynSmem, st>>>(a, t, mixed_const(a), parity, l);
     return launch_status();
 }
 
-template <int W, int MINB, bool COMP>
-int launch_tiled_comp(const pp_fused_args& a, const pp_tiling& t, int parity, const Launch& l,
-                      cudaStream_t st) {
+template <int NW, int W, int MINB, bool COMP>
+int launch_tiled_nw(const pp_fused_args& a, const pp_tiling& t, int parity, const Launch& l,
+                    cudaStream_t st) {
     const bool corr = a.stiffness_corrections != nullptr;
     const bool types = a.bond_types != nullptr;
-    if (!corr && !types) return launch_tiled_instance<false, false, COMP, W, MINB>(a, t, parity, l, st);
-    if (corr && !types) return launch_tiled_instance<true, false, COMP, W, MINB>(a, t, parity, l, st);
-    if (!corr && types) return launch_tiled_instance<false, true, COMP, W, MINB>(a, t, parity, l, st);
-    return launch_tiled_instance<true, true, COMP, W, MINB>(a, t, parity, l, st);
+    if (!corr && !types)
+        return launch_tiled_instance<NW, false, false, COMP, W, MINB>(a, t, parity, l, st);
+    if (corr && !types)
+        return launch_tiled_instance<NW, true, false, COMP, W, MINB>(a, t, parity, l, st);
+    if (!corr && types)
+        return launch_tiled_instance<NW, false, true, COMP, W, MINB>(a, t, parity, l, st);
+    return launch_tiled_instance<NW, true, true, COMP, W, MINB>(a, t, parity, l, st);
 }
 
-// All kernel instances of one tile shape (W warps, register budget MINB).
+// All kernel instances of one tile shape (W warps, register budget MINB):
+// rows of at most 32, 64, 128 or 256 entries (max_neigh).
 template <int W, int MINB>
 int launch_tiled_shape(const pp_fused_args& a, const pp_tiling& t, int parity, const Launch& l,
                        cudaStream_t st) {
-    if (a.flags & PP_FLAG_COMPENSATED) return launch_tiled_comp<W, MINB, true>(a, t, parity, l, st);
-    return launch_tiled_comp<W, MINB, false>(a, t, parity, l, st);
+    const bool comp = (a.flags & PP_FLAG_COMPENSATED) != 0;
+#define PP_TILED_NW(N)                                                        \
+    if (a.max_neigh <= 16 * (N))                                              \
+        return comp ? launch_tiled_nw<N, W, MINB, true>(a, t, parity, l, st) \
+                    : launch_tiled_nw<N, W, MINB, false>(a, t, parity, l, st);
+    PP_TILED_NW(2)
+    PP_TILED_NW(4)
+    PP_TILED_NW(8)
+    PP_TILED_NW(16)
+#undef PP_TILED_NW
+    return PP_ERROR_UNSUPPORTED;  // max_neigh > 256
 }
 
 // Launchers of the tile shapes, one translation unit each (pp_tiled_v*.cu).

@@ -40,15 +40,33 @@ __device__ __forceinline__ bool valid_node(int j, int n) { return j >= 0 && j < 
 // a power of two >= 2 * the sorted capacity sc), then sorted (bitonic) into
 // the halo.  Each node's row length (intact slots rounded up to 16) goes
 // to row_off[i + 1] in units of 16 entries.
+// Fixed-point position of reference node o (the formula of pp_mixed_pack).
+__device__ __forceinline__ int fixed_pos(const double* r0, int64_t o, int d, const double* origin,
+                                         double inv_scale) {
+    return (int)llrint((r0[3 * o + d] - origin[d]) * inv_scale);
+}
+
+struct Frame {
+    double origin[3];
+    double inv_scale;  // 1 / pos_scale (a power of two: exact)
+};
+
+// The largest |q - ref| a staged position may have (exact float
+// conversion of q - ref by the 1.5 * 2^23 exponent trick).
+constexpr int kRefReach = (1 << 22) - 1;
+
 __global__ void k_tile_halos(const int32_t* __restrict__ nlist, int L, int n,
                              const int32_t* __restrict__ perm, const int32_t* __restrict__ inv,
                              const int32_t* __restrict__ tile_start, int halo_cap, int hc,
                              int sc, int32_t* __restrict__ halo, int32_t* __restrict__ halo_count,
-                             int32_t* __restrict__ own_off, int32_t* __restrict__ row_off) {
+                             int32_t* __restrict__ own_off, int32_t* __restrict__ row_off,
+                             int32_t* __restrict__ tile_ref, const double* __restrict__ r0,
+                             Frame frame) {
     extern __shared__ int smem[];
     int* hs = smem;        // hash slots, -1 = empty
     int* keys = smem + hc;  // compacted, then sorted
-    __shared__ int count, placed;
+    __shared__ int count, placed, far;
+    __shared__ int qlo[3], qhi[3];
     const int t = blockIdx.x;
     const int n0 = tile_start[t], n1 = tile_start[t + 1];
     const int nt = n1 - n0;
@@ -56,6 +74,11 @@ __global__ void k_tile_halos(const int32_t* __restrict__ nlist, int L, int n,
     if (threadIdx.x == 0) {
         count = 0;
         placed = 0;
+        far = 0;
+        for (int d = 0; d < 3; ++d) {
+            qlo[d] = 0x7FFFFFFF;
+            qhi[d] = -0x7FFFFFFF;
+        }
         if (t == 0) row_off[0] = 0;
     }
     __syncthreads();
@@ -73,7 +96,15 @@ __global__ void k_tile_halos(const int32_t* __restrict__ nlist, int L, int n,
             h = (h + 1) & (hc - 1);
         }
     };
-    for (int li = threadIdx.x; li < nt; li += blockDim.x) insert(n0 + li);
+    for (int li = threadIdx.x; li < nt; li += blockDim.x) {
+        insert(n0 + li);
+        const int64_t o = perm[n0 + li];
+        for (int d = 0; d < 3; ++d) {
+            const int q = fixed_pos(r0, o, d, frame.origin, frame.inv_scale);
+            atomicMin(&qlo[d], q);
+            atomicMax(&qhi[d], q);
+        }
+    }
     // bonds: warp per node, lanes over slots; row lengths on the way
     const int lane = threadIdx.x & 31;
     for (int li = threadIdx.x >> 5; li < nt; li += blockDim.x >> 5) {
@@ -116,11 +147,31 @@ __global__ void k_tile_halos(const int32_t* __restrict__ nlist, int L, int n,
             }
             __syncthreads();
         }
+    // reference point: the middle of the tile's own bounding box; every
+    // halo node must lie within kRefReach fixed-point steps of it
+    int ref[3];
+    for (int d = 0; d < 3; ++d)
+        ref[d] = nt > 0 ? (int)(((long long)qlo[d] + (long long)qhi[d]) >> 1) : 0;
+    for (int k = threadIdx.x; k < nh; k += blockDim.x) {
+        const int64_t o = perm[keys[k]];
+        for (int d = 0; d < 3; ++d) {
+            const long long dq =
+                (long long)fixed_pos(r0, o, d, frame.origin, frame.inv_scale) - ref[d];
+            if (dq > kRefReach || dq < -kRefReach) far = 1;
+        }
+    }
+    __syncthreads();
+    if (far) {
+        if (threadIdx.x == 0) halo_count[t] = halo_cap + 1;
+        return;
+    }
     int32_t* out = halo + (int64_t)t * halo_cap;
     for (int k = threadIdx.x; k < nh; k += blockDim.x) out[k] = keys[k];
     if (threadIdx.x == 0) {
         halo_count[t] = nh;
         own_off[t] = nt > 0 ? lower_bound(keys, nh, n0) : 0;
+        for (int d = 0; d < 3; ++d) tile_ref[4 * t + d] = ref[d];
+        tile_ref[4 * t + 3] = 0;
     }
 }
 
@@ -162,8 +213,8 @@ __global__ void k_scan_rows(int32_t* __restrict__ row_off, int n) {
 
 // One CTA per tile: the rows of its nodes (warp per node) from the
 // reference row, in slot order, with halo indices found in the sorted halo
-// (shared memory); padding entries 0xFFFF / slot 0xFF.  Also the initial
-// intact count per node.
+// (shared memory), stored as 16 x index; padding entries hold the node's
+// own entry, slot 0xFF.  Also the initial intact count per node.
 __global__ void k_tile_rows(const int32_t* __restrict__ nlist, int L, int n,
                             const int32_t* __restrict__ bond_types,
                             const int32_t* __restrict__ regimes,
@@ -171,14 +222,17 @@ __global__ void k_tile_rows(const int32_t* __restrict__ nlist, int L, int n,
     extern __shared__ int hl[];
     const int tile = blockIdx.x;
     const int n0 = t.tile_start[tile], n1 = t.tile_start[tile + 1];
-    const int nh = t.halo_count[tile];
+    // a count above the capacity (an unsplit tile) never addresses past it
+    const int nh = min(max(t.halo_count[tile], 0), t.halo_cap);
     const int32_t* src = t.halo + (int64_t)tile * t.halo_cap;
     for (int k = threadIdx.x; k < nh; k += blockDim.x) hl[k] = src[k];
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
+    const int own0 = t.own_off[tile];
     for (int i = n0 + (threadIdx.x >> 5); i < n1; i += blockDim.x >> 5) {
         const int o = t.perm[i];
+        const uint16_t self = (uint16_t)(16 * (own0 + (i - n0)));
         const int64_t ref = (int64_t)o * L;
         const int64_t rowE = 16 * (int64_t)t.row_off[i];
         const int len = 16 * (t.row_off[i + 1] - t.row_off[i]);
@@ -191,8 +245,9 @@ __global__ void k_tile_rows(const int32_t* __restrict__ nlist, int L, int n,
             if (ok) {
                 const int p = base + __popc(bal & below);
                 const int64_t pos = rowE + entry_pos(p);
-                const int e = lower_bound(hl, nh, t.inv[j]);
-                t.entry[pos] = (uint16_t)(e < nh ? e : 0xFFFF);
+                const int key = t.inv[j];
+                const int e = lower_bound(hl, nh, key);
+                t.entry[pos] = e < nh && hl[e] == key ? (uint16_t)(16 * e) : self;
                 t.slot[pos] = (uint8_t)s;
                 if (t.bond_type) t.bond_type[pos] = (uint8_t)bond_types[ref + s];
                 if (t.regime) t.regime[pos] = (uint8_t)regimes[ref + s];
@@ -202,7 +257,7 @@ __global__ void k_tile_rows(const int32_t* __restrict__ nlist, int L, int n,
         }
         for (int p = base + lane; p < len; p += 32) {
             const int64_t pos = rowE + entry_pos(p);
-            t.entry[pos] = 0xFFFF;
+            t.entry[pos] = self;
             t.slot[pos] = 0xFF;
             if (t.bond_type) t.bond_type[pos] = 0;
             if (t.regime) t.regime[pos] = 0;
@@ -227,21 +282,30 @@ __global__ void k_tile_nodes(const double* __restrict__ r0, const double* __rest
     if (t.node_instance) t.node_instance[i] = node_instance[o];
 }
 
-// Bonds broken since pp_tile_rows (entry 0xFFFF, slot != 0xFF) become -1
-// in the reference neighbour list; regimes are copied back.  Warp per
-// internal node.
+// Bonds broken since pp_tile_rows (an entry equal to the node's own entry,
+// slot != 0xFF) become -1 in the reference neighbour list; regimes are
+// copied back.  Warp per internal node (its tile found by bisection).
 __global__ void k_tile_export(int32_t* __restrict__ nlist, int32_t* __restrict__ regimes, int L,
                               int n, pp_tiling t) {
     const int lane = threadIdx.x & 31;
     const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (i >= n) return;
+    int lo = 0, hi = t.ntiles;  // the tile with tile_start[tile] <= i
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (t.tile_start[mid] <= i)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    const int self = 16 * (t.own_off[lo] + (i - t.tile_start[lo]));
     const int64_t ref = (int64_t)t.perm[i] * L;
     const int64_t rowE = 16 * (int64_t)t.row_off[i];
     const int len = 16 * (t.row_off[i + 1] - t.row_off[i]);
     for (int q = lane; q < len; q += 32) {
         const int s = t.slot[rowE + q];
         if (s == 0xFF || s >= L) continue;
-        if (t.entry[rowE + q] == 0xFFFF) nlist[ref + s] = -1;
+        if (t.entry[rowE + q] == self) nlist[ref + s] = -1;
         if (regimes && t.regime) regimes[ref + s] = t.regime[rowE + q];
     }
 }
@@ -257,7 +321,8 @@ int check_tiling(const pp_fused_args& a, const pp_tiling* t) {
     if (t->ntiles < 0 || (a.nnodes > 0 && t->ntiles < 1)) return PP_ERROR_INVALID_VALUE;
     if (t->halo_cap < 1 || t->halo_cap > PP_TILE_HALO_MAX) return PP_ERROR_INVALID_VALUE;
     if (!t->perm || !t->inv || !t->tile_start || !t->halo || !t->halo_count || !t->own_off ||
-        !t->row_off || !t->r0 || !t->bc_values || !t->fc_values || !t->n_neigh || !t->sched)
+        !t->tile_ref || !t->row_off || !t->r0 || !t->bc_values || !t->fc_values ||
+        !t->n_neigh || !t->sched)
         return PP_ERROR_INVALID_VALUE;
     return PP_SUCCESS;
 }
@@ -303,15 +368,18 @@ extern "C" int pp_tile_halos(const pp_fused_args* args, const pp_tiling* t, void
     int rc = check_tiling(a, t);
     if (rc != PP_SUCCESS) return rc;
     if (a.nnodes == 0) return PP_SUCCESS;
-    if (!a.nlist) return PP_ERROR_INVALID_VALUE;
+    if (!a.nlist || !a.r0 || !(a.pos_scale > 0.0)) return PP_ERROR_INVALID_VALUE;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Frame frame;
+    for (int d = 0; d < 3; ++d) frame.origin[d] = a.pos_origin[d];
+    frame.inv_scale = 1.0 / a.pos_scale;
     const int sc = next_pow2(t->halo_cap);
     const int hc = 2 * (sc < 512 ? 512 : sc);
     const size_t bytes = (size_t)(hc + sc) * sizeof(int);
     if (bytes > 48 * 1024) return PP_ERROR_UNSUPPORTED;
     k_tile_halos<<<t->ntiles, kThreads, bytes, st>>>(
         a.nlist, a.max_neigh, a.nnodes, t->perm, t->inv, t->tile_start, t->halo_cap, hc, sc,
-        t->halo, t->halo_count, t->own_off, t->row_off);
+        t->halo, t->halo_count, t->own_off, t->row_off, t->tile_ref, a.r0, frame);
     rc = launch_status();
     if (rc != PP_SUCCESS) return rc;
     k_scan_rows<<<1, 1024, 0, st>>>(t->row_off, a.nnodes);

@@ -114,11 +114,11 @@ class DeviceTiling:
     :arg device: torch device.
     """
 
-    def __init__(self, perm, tile_start, device, halo_cap=HALO_CAP):
+    def __init__(self, perm, tile_start, device, halo_cap=None):
         import torch
         self._torch = torch
         self.device = device
-        self.halo_cap = int(halo_cap)
+        self.halo_cap = int(HALO_CAP if halo_cap is None else halo_cap)
         self.perm = np.ascontiguousarray(perm, dtype=np.int32)
         self.tile_start = np.ascontiguousarray(tile_start, dtype=np.int32)
         n = self.perm.size
@@ -150,6 +150,7 @@ class DeviceTiling:
             self.halo_d = self._t((max(nt, 1) * self.halo_cap,), i32)
             self.halo_count_d = self._t((max(nt, 1),), i32)
             self.own_off_d = self._t((max(nt, 1),), i32)
+            self.tile_ref_d = self._t((max(nt, 1) * 4,), i32)
             self.row_off_d = self._t((n + 1,), i32)
             self.n_neigh_d = self._t((max(n, 1),), i32)
             self.sched_d = torch.zeros(2, dtype=i32, device=self.device)
@@ -166,6 +167,7 @@ class DeviceTiling:
             s.halo = self.halo_d.data_ptr()
             s.halo_count = self.halo_count_d.data_ptr()
             s.own_off = self.own_off_d.data_ptr()
+            s.tile_ref = self.tile_ref_d.data_ptr()
             s.row_off = self.row_off_d.data_ptr()
             s.n_neigh = self.n_neigh_d.data_ptr()
             s.sched = self.sched_d.data_ptr()

@@ -62,10 +62,10 @@ def test_struct_layout_matches_header():
     assert f["bond_length"].offset == f["bond_types"].offset + 8
     assert f["pos_origin"].offset + 24 == f["tiling"].offset
     assert f["tiling"].offset + 8 == ctypes.sizeof(_lib.FusedArgs)
-    # pp_tiling: 2 int32 then 18 pointers
-    assert ctypes.sizeof(_lib.Tiling) == 2 * 4 + 18 * 8
+    # pp_tiling: 2 int32 then 19 pointers
+    assert ctypes.sizeof(_lib.Tiling) == 2 * 4 + 19 * 8
     assert _lib.Tiling.perm.offset == 8
-    assert _lib.Tiling.sched.offset == 8 + 17 * 8
+    assert _lib.Tiling.sched.offset == 8 + 18 * 8
 
 
 def test_struct_layout_matches_c_compiler(tmp_path):
@@ -80,8 +80,8 @@ def test_struct_layout_matches_c_compiler(tmp_path):
     checks = {"pp_fused_args": (_lib.FusedArgs, ("variant", "dt", "nlist",
                                                 "rec", "pos_origin",
                                                 "tiling")),
-              "pp_tiling": (_lib.Tiling, ("perm", "entry", "correction",
-                                          "n_neigh", "sched")),
+              "pp_tiling": (_lib.Tiling, ("perm", "tile_ref", "entry",
+                                          "correction", "n_neigh", "sched")),
               "pp_corrections_args": (_lib.CorrectionsArgs, ("r0",)),
               "pp_write_sums_args": (_lib.WriteSumsArgs, ("u", "sums")),
               "pp_adjoint_args": (_lib.AdjointArgs, ("r0", "stiffness"))}
