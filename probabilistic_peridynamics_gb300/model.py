@@ -112,6 +112,218 @@ def create_crack(crack, nlist, n_neigh):
                 n_neigh[a] = cnt - 1
 
 
+
+def _given_array(name, value, shape, dtype, shape_text):
+    """An array a caller supplied in place of one :class:`Model` would
+    compute: its type and shape are checked, its use is announced with a
+    warning (as PeriPy announces it) and it is converted to ``dtype``."""
+    if type(value) != np.ndarray:
+        raise TypeError("{} type is wrong (expected {}, got {})".format(
+            name, np.ndarray, type(value)))
+    if np.shape(value) != shape:
+        raise ValueError("{} shape is wrong, and must be {} (expected {}, "
+                         "got {})".format(name, shape_text, shape,
+                                          np.shape(value)))
+    warnings.warn("Reading {} from argument.".format(name))
+    return value.astype(dtype)
+
+
+def _connectivity_pair(connectivity):
+    """``(nlist, n_neigh)`` from a connectivity argument (a 2-tuple)."""
+    if type(connectivity) != tuple:
+        raise TypeError("connectivity type is wrong (expected {} or {}, got "
+                        "{})".format(tuple, type(None), type(connectivity)))
+    if len(connectivity) != 2:
+        raise ValueError("connectivity size is wrong (expected 2, got "
+                         "{})".format(len(connectivity)))
+    return connectivity
+
+
+def _schedule(name, value, first_step, steps):
+    """Per-step boundary-condition magnitudes: zeros by default, else a
+    float64 copy of an array that covers ``steps`` steps."""
+    last = first_step + steps - 1
+    if value is None:
+        return np.zeros(last, dtype=np.float64)
+    if type(value) != np.ndarray:
+        raise TypeError("{} type is wrong (expected {}, got {})".format(
+            name, np.ndarray, type(value)))
+    if len(value) < steps:
+        raise ValueError("{} length must be equal to or greater than "
+                         "(first_step + steps - 1), (expected {}, got "
+                         "{})".format(name, last, len(value)))
+    return value.astype(np.float64)
+
+
+class DamageModel(tuple):
+    """``(bond_stiffness, critical_stretch, plus_cs, nbond_types,
+    nregimes)`` of a normalised damage model (see :func:`damage_model`)."""
+
+    __slots__ = ()
+
+
+def _nlinear(k, s):
+    """Tables of an n-linear model, rows = bond types: the stretches of a
+    row must not decrease; ``plus_cs`` keeps the force continuous across
+    regimes (``plus_cs[:, r] = plus_cs[:, r-1] + k[:, r-1] s[:, r-1] -
+    k[:, r] s[:, r-1]``, peripy/model.py:1031-1039)."""
+    for row in s:
+        if not np.all(row[:-1] <= row[1:]):  # NaN fails too
+            raise DamageModelError(row)
+    from .pointset import nlinear_tables
+    return nlinear_tables(k, s)[2]
+
+
+#: How each layout of (bond_stiffness, critical_stretch) is normalised:
+#: (number of bond types, number of regimes, builder of (k, s, plus_cs)).
+#: Layouts: a Python or NumPy float; an array of shape (1,); a 0-d array;
+#: one stiffness per bond type (shape (T, 1)); one bond type with R
+#: regimes (shape (R,)); T bond types with R regimes (shape (T, R)).
+_DAMAGE_LAYOUTS = {
+    "scalar": (lambda k: 1, lambda k: 1,
+               lambda k, s: (np.float64(k), np.float64(s), None)),
+    "single": (lambda k: 1, lambda k: 1,
+               lambda k, s: (np.float64(k[0]), np.float64(s[0]), None)),
+    "0d": (lambda k: 1, lambda k: 1,
+           lambda k, s: (np.float64(k), np.array(s), None)),
+    "types": (lambda k: len(k), lambda k: 1,
+              lambda k, s: (np.array(k, dtype=np.float64),
+                            np.array(s, dtype=np.float64),
+                            np.zeros(len(k), dtype=np.float64))),
+    "regimes": (lambda k: 1, lambda k: len(k),
+                lambda k, s: (np.array(k, dtype=np.float64),
+                              np.array(s, dtype=np.float64),
+                              _nlinear(np.array([k], dtype=np.float64),
+                                       np.array([s], dtype=np.float64))[0])),
+    "table": (lambda k: np.shape(k)[0], lambda k: np.shape(k)[1],
+              lambda k, s: (np.array(k, dtype=np.float64),
+                            np.array(s, dtype=np.float64),
+                            _nlinear(np.array(k, dtype=np.float64),
+                                     np.array(s, dtype=np.float64)))),
+}
+
+
+def _damage_layout(bond_stiffness, critical_stretch):
+    if type(bond_stiffness) != type(critical_stretch):
+        raise TypeError(
+            "bond_stiffness must be the same type as critical_stretch "
+            "(expected {}, got {})".format(type(critical_stretch),
+                                           type(bond_stiffness)))
+    if type(bond_stiffness) in (float, np.float64):
+        return "scalar"
+    if type(bond_stiffness) not in (list, np.ndarray):
+        raise TypeError(
+            "Type of bond_stiffness and critical_stretch is not supported "
+            "(expected {} or {}, got {})".format(float, np.ndarray,
+                                                  type(bond_stiffness)))
+    shape = np.shape(bond_stiffness)
+    if shape != np.shape(critical_stretch):
+        raise ValueError(
+            "The shape of bond_stiffness must be equal to the shape of "
+            "critical_stretch (expected {}, got {})".format(
+                np.shape(critical_stretch), shape))
+    if shape == (1,):
+        return "single"
+    if shape == ():
+        return "0d"
+    inner = np.shape(bond_stiffness[0])
+    if inner == (1,):
+        return "types"
+    return "regimes" if inner == () else "table"
+
+
+def damage_model(bond_stiffness, critical_stretch):
+    """Normalise a damage model as PeriPy's ``Model`` takes it
+    (``peripy/model.py:941-1091``): a float (PMB), or arrays of stiffness
+    and critical stretch per bond type and/or regime (n-linear).
+
+    :returns: :class:`DamageModel` ``(bond_stiffness, critical_stretch,
+        plus_cs, nbond_types, nregimes)``: scalars (``plus_cs`` None) for
+        one type and one regime, else float64 tables; the counts as
+        ``np.intc``.
+    """
+    ntypes, nregimes, build = _DAMAGE_LAYOUTS[
+        _damage_layout(bond_stiffness, critical_stretch)]
+    k, s, plus_cs = build(bond_stiffness, critical_stretch)
+    if np.any(s < 0):
+        raise ValueError("critical_stretch values must not be < 0, "
+                         "(got {})".format(s))
+    return DamageModel((k, s, plus_cs, np.intc(ntypes(bond_stiffness)),
+                        np.intc(nregimes(bond_stiffness))))
+
+
+def _check_node_function(name, function, x):
+    """A user function of a node's coordinates must return a list of 3."""
+    if not callable(function):
+        raise TypeError("{} must be a *function*.".format(name))
+    value = function(x)
+    if type(value) is not list:
+        raise TypeError("{} must be a function that returns a *list*."
+                        .format(name))
+    if len(value) != 3:
+        if name == 'is_tip':
+            raise TypeError("{} must be a function that returns a list of "
+                            "length *3* of ints or strings or tuples of ints "
+                            "or strings")
+        raise TypeError("{} must be a function that returns a list of "
+                        "length *3* of floats or None")
+
+
+def boundary_conditions(coords, volume, is_displacement_boundary,
+                        is_force_boundary, is_tip):
+    """Boundary-condition arrays and tips from the user's node functions
+    (``peripy/model.py:1093-1212``).
+
+    Each function is evaluated once per node; its per-component values
+    (None: no condition) are gathered into arrays, and the arrays are
+    formed with NumPy.  A force value is applied per unit volume of its
+    node and shared equally among the nodes that carry any force condition.
+
+    :returns: ``(bc_types, bc_values, force_bc_types, force_bc_values,
+        tip_types, ntips)``; ``tip_types[tip]`` lists the ``(node,
+        component)`` pairs of each tip in node, then component order
+        (members of a tuple in their order) and ``ntips`` counts them, with
+        ``ntips['model']`` the number of nodes.
+    """
+    funcs = (('is_displacement_boundary', is_displacement_boundary),
+             ('is_force_boundary', is_force_boundary), ('is_tip', is_tip))
+    for name, f in funcs:
+        _check_node_function(name, f, coords[0][:])
+    n = coords.shape[0]
+    disp = np.zeros((n, 3))
+    force = np.zeros((n, 3))
+    bc_types = np.zeros((n, 3), dtype=np.intc)
+    force_bc_types = np.zeros((n, 3), dtype=np.intc)
+    tips = {}
+    ntips = {'model': n}
+    for i in range(n):
+        x = coords[i][:]
+        for j, v in enumerate(is_displacement_boundary(x)):
+            if v is not None:
+                disp[i, j] = v
+                bc_types[i, j] = 1
+        for j, v in enumerate(is_force_boundary(x)):
+            if v is not None:
+                force[i, j] = v
+                force_bc_types[i, j] = 1
+        for j, t in enumerate(is_tip(x)):
+            if t is None:
+                continue
+            for name in (t if type(t) is tuple else (t,)):
+                tips.setdefault(str(name), []).append((i, j))
+    for name, entries in tips.items():
+        ntips[name] = len(entries)
+    bc_values = disp
+    # per unit volume of the node, then shared among the force nodes
+    force_bc_values = np.where(force_bc_types == 1,
+                               force / volume[:, None], 0.0)
+    force_nodes = int(np.count_nonzero(force_bc_types.any(axis=1)))
+    if force_nodes:
+        force_bc_values = force_bc_values / force_nodes
+    return (bc_types, bc_values, force_bc_types, force_bc_values, tips,
+            ntips)
+
+
 class Model(object):
     """A bond-based peridynamics model (``peripy/model.py:24``)."""
 
@@ -147,16 +359,9 @@ class Model(object):
             self.volume = self._volume(transfinite, volume_total)
             if self.write_path is not None:
                 write_array(self.write_path, "volume", self.volume)
-        elif type(volume) == np.ndarray:
-            if np.shape(volume) != (self.nnodes, ):
-                raise ValueError("volume shape is wrong, and must be "
-                                 "(nnodes, ) (expected {}, got {})".format(
-                                     (self.nnodes, ), np.shape(volume)))
-            warnings.warn("Reading volume from argument.")
-            self.volume = volume.astype(np.float64)
         else:
-            raise TypeError("volume type is wrong (expected {}, got "
-                            "{})".format(type(volume), np.ndarray))
+            self.volume = _given_array("volume", volume, (self.nnodes,),
+                                       np.float64, "(nnodes, )")
 
         if volume_correction is not None:
             if not ((type(node_radius) == float)
@@ -181,47 +386,26 @@ class Model(object):
                 write_array(self.write_path, "nlist", nlist)
                 write_array(self.write_path, "n_neigh", n_neigh)
         else:
-            if type(family) == np.ndarray:
-                if np.shape(family) != (self.nnodes, ):
-                    raise ValueError("family shape is wrong, and must be "
-                                     "(nnodes, ) (expected {}, got {})".format(
-                                         (self.nnodes, ), np.shape(family)))
-                warnings.warn("Reading family from argument.")
-                self.family = family.astype(np.intc)
-            else:
-                raise TypeError("family type is wrong (expected {}, got "
-                                "{})".format(type(family), np.ndarray))
-            if type(connectivity) == tuple:
-                if len(connectivity) != 2:
-                    raise ValueError("connectivity size is wrong (expected 2,"
-                                     " got {})".format(len(connectivity)))
-                warnings.warn("Reading connectivity from argument.")
-                nlist, n_neigh = connectivity
-                nlist = nlist.astype(np.intc)
-                n_neigh = n_neigh.astype(np.intc)
-                self.max_neighbours = np.intc(np.shape(nlist)[1])
-                if not integrator.context:
-                    if self.max_neighbours != self.family.max():
-                        raise ValueError(
-                            "max_neighbours, which is equal to the size of "
-                            "axis 1 of nlist is wrong (expected "
-                            "max_neighbours = np.shape(nlist)[1] = "
-                            "family.max() = {}, got {})".format(
-                                self.family.max(), self.max_neighbours))
-                else:
-                    test = self.max_neighbours - 1
-                    if self.max_neighbours & test:
-                        raise ValueError(
-                            "max_neighbours, which is equal to the size of "
-                            "axis 1 of nlist is wrong (expected "
-                            "max_neighbours = np.shape(nlist)[1] = {}, got "
-                            "{})".format(
-                                1 << (int(self.family.max() - 1)).bit_length(),
-                                self.max_neighbours))
-            else:
-                raise TypeError("connectivity type is wrong (expected {} or"
-                                " {}, got {})".format(
-                                    tuple, type(None), type(connectivity)))
+            self.family = _given_array("family", family, (self.nnodes,),
+                                       np.intc, "(nnodes, )")
+            nlist, n_neigh = _connectivity_pair(connectivity)
+            warnings.warn("Reading connectivity from argument.")
+            nlist = nlist.astype(np.intc)
+            n_neigh = n_neigh.astype(np.intc)
+            self.max_neighbours = np.intc(np.shape(nlist)[1])
+            # the row width each integrator family works on: family.max()
+            # for the CPU layout, a power of two for device integrators
+            width = (1 << (int(self.family.max() - 1)).bit_length()
+                     if integrator.context else self.family.max())
+            fits = (self.max_neighbours & (self.max_neighbours - 1) == 0
+                    if integrator.context
+                    else self.max_neighbours == width)
+            if not fits:
+                raise ValueError(
+                    "max_neighbours, which is equal to the size of axis 1 "
+                    "of nlist is wrong (expected max_neighbours = "
+                    "np.shape(nlist)[1] = {}, got {})".format(
+                        width, self.max_neighbours))
 
         if np.any(self.family == 0):
             raise FamilyError(self.family)
@@ -252,46 +436,28 @@ class Model(object):
                     and self.write_path is not None):
                 write_array(self.write_path, "stiffness_corrections",
                             self.stiffness_corrections)
-        elif type(stiffness_corrections) == np.ndarray:
-            if np.shape(stiffness_corrections) != (
-                    self.nnodes, self.max_neighbours):
-                raise ValueError("stiffness_corrections shape is wrong, "
-                                 "and must be (nnodes, max_neighbours) "
-                                 "(expected {}, got {})".format(
-                                     (self.nnodes, self.max_neighbours),
-                                     np.shape(stiffness_corrections)))
-            warnings.warn("Reading stiffness_corrections from argument.")
-            self.stiffness_corrections = stiffness_corrections.astype(
-                np.float64)
         else:
-            raise TypeError("stiffness_corrections type is wrong (expected {}"
-                            ", got {})".format(np.ndarray,
-                                               type(stiffness_corrections)))
+            self.stiffness_corrections = _given_array(
+                "stiffness_corrections", stiffness_corrections,
+                (self.nnodes, self.max_neighbours), np.float64,
+                "(nnodes, max_neighbours)")
 
         if is_bond_type is None:
             def is_bond_type(x, y):
                 return 0
 
         (self.bond_stiffness, self.critical_stretch, self.plus_cs,
-         self.nbond_types, self.nregimes) = self._set_damage_model(
+         self.nbond_types, self.nregimes) = damage_model(
              bond_stiffness, critical_stretch)
 
         if bond_types is None:
             self.bond_types = self._set_bond_types(
                 self.initial_connectivity, is_bond_type, self.nbond_types,
                 self.nregimes)
-        elif type(bond_types) == np.ndarray:
-            if np.shape(bond_types) != (self.nnodes, self.max_neighbours):
-                raise ValueError("bond_types shape is wrong, "
-                                 "and must be (nnodes, max_neighbours) "
-                                 "(expected {}, got {})".format(
-                                     (self.nnodes, self.max_neighbours),
-                                     np.shape(bond_types)))
-            warnings.warn("Reading bond_types from argument.")
-            self.bond_types = bond_types.astype(np.intc)
         else:
-            raise TypeError("bond_types type is wrong (expected {}"
-                            ", got {})".format(np.ndarray, type(bond_types)))
+            self.bond_types = _given_array(
+                "bond_types", bond_types, (self.nnodes, self.max_neighbours),
+                np.intc, "(nnodes, max_neighbours)")
 
         self.densities = self._set_densities(density, is_density)
 
@@ -480,172 +646,15 @@ class Model(object):
         return bond_types
 
     def _set_damage_model(self, bond_stiffness, critical_stretch):
-        """Normalise the damage model (``peripy/model.py:941-1091``).
-
-        :returns: ``(bond_stiffness, critical_stretch, plus_cs, nbond_types,
-            nregimes)``; ``plus_cs[r] = plus_cs[r-1] + k[r-1]*s[r-1] -
-            k[r]*s[r-1]`` so the n-linear force is continuous.
-        """
-        if type(bond_stiffness) != type(critical_stretch):
-            raise TypeError(
-                "bond_stiffness must be the same type as critical_stretch "
-                "(expected {}, got {})".format(type(critical_stretch),
-                                               type(bond_stiffness)))
-        if type(bond_stiffness) in (list, np.ndarray):
-            if np.shape(bond_stiffness) != np.shape(critical_stretch):
-                raise ValueError(
-                    "The shape of bond_stiffness must be equal to the shape "
-                    "of critical_stretch (expected {}, got {})".format(
-                        np.shape(critical_stretch), np.shape(bond_stiffness)))
-            if np.shape(bond_stiffness) == (1,):
-                nregimes = 1
-                nbond_types = 1
-                bond_stiffness = np.float64(bond_stiffness[0])
-                critical_stretch = np.float64(critical_stretch[0])
-                plus_cs = None
-            elif np.shape(bond_stiffness) == ():
-                nregimes = 1
-                nbond_types = 1
-                bond_stiffness = np.float64(bond_stiffness)
-                critical_stretch = np.array(critical_stretch)
-                plus_cs = None
-            elif np.shape(bond_stiffness[0]) == (1,):
-                nregimes = 1
-                nbond_types = np.shape(bond_stiffness)[0]
-                bond_stiffness = np.array(bond_stiffness, dtype=np.float64)
-                critical_stretch = np.array(critical_stretch,
-                                            dtype=np.float64)
-                plus_cs = np.zeros(nbond_types).astype(np.float64)
-            elif np.shape(bond_stiffness[0]) == ():
-                nbond_types = 1
-                nregimes = np.shape(bond_stiffness)[0]
-                if not all(critical_stretch[i] <= critical_stretch[i + 1]
-                           for i in range(nregimes - 1)):
-                    raise DamageModelError(critical_stretch)
-                bond_stiffness = np.array(bond_stiffness, dtype=np.float64)
-                critical_stretch = np.array(critical_stretch,
-                                            dtype=np.float64)
-                plus_cs = np.zeros(nregimes)
-                c_prev = 0.0
-                plus_cs[0] = c_prev
-                for r in range(1, nregimes):
-                    c_i = (c_prev
-                           + (bond_stiffness[r - 1] * critical_stretch[r - 1])
-                           - (bond_stiffness[r] * critical_stretch[r - 1]))
-                    plus_cs[r] = c_i
-                    c_prev = c_i
-                plus_cs = plus_cs.astype(np.float64)
-            else:
-                nregimes = np.shape(bond_stiffness)[1]
-                nbond_types = np.shape(bond_stiffness)[0]
-                for i in range(nbond_types):
-                    if not all(critical_stretch[i][j] <=
-                               critical_stretch[i][j + 1]
-                               for j in range(nregimes - 1)):
-                        raise DamageModelError(critical_stretch[i])
-                bond_stiffness = np.array(bond_stiffness, dtype=np.float64)
-                critical_stretch = np.array(critical_stretch,
-                                            dtype=np.float64)
-                plus_cs = np.zeros((nbond_types, nregimes))
-                c_prev = np.zeros(nbond_types)
-                plus_cs[:, 0] = c_prev
-                for r in range(1, nregimes):
-                    c_i = (c_prev
-                           + (bond_stiffness[:, r - 1] *
-                              critical_stretch[:, r - 1])
-                           - (bond_stiffness[:, r] *
-                              critical_stretch[:, r - 1]))
-                    plus_cs[:, r] = c_i
-                    c_prev = c_i
-                plus_cs = plus_cs.astype(np.float64)
-        elif type(bond_stiffness) in (float, np.float64):
-            nregimes = 1
-            nbond_types = 1
-            bond_stiffness = np.float64(bond_stiffness)
-            critical_stretch = np.float64(critical_stretch)
-            plus_cs = None
-        else:
-            raise TypeError(
-                "Type of bond_stiffness and critical_stretch is not supported "
-                "(expected {} or {}, got {})".format(
-                    float, np.ndarray, type(bond_stiffness)))
-        nregimes = np.intc(nregimes)
-        nbond_types = np.intc(nbond_types)
-        if np.any(critical_stretch < 0):
-            raise ValueError("critical_stretch values must not be < 0, "
-                             "(got {})".format(critical_stretch))
-        return (bond_stiffness, critical_stretch, plus_cs, nbond_types,
-                nregimes)
+        """The damage model as :func:`damage_model` normalises it."""
+        return damage_model(bond_stiffness, critical_stretch)
 
     def _set_boundary_conditions(self, is_displacement_boundary,
                                  is_force_boundary, is_tip):
-        """BC arrays and tip lists (``peripy/model.py:1093-1212``)."""
-        functions = {'is_displacement_boundary': is_displacement_boundary,
-                     'is_force_boundary': is_force_boundary,
-                     'is_tip': is_tip}
-        for function in functions:
-            if not callable(functions[function]):
-                raise TypeError("{} must be a *function*.".format(function))
-            if type(functions[function](self.coords[0][:])) is not list:
-                raise TypeError(
-                    "{} must be a function that returns a *list*.".format(
-                        function))
-            if len(functions[function](self.coords[0][:])) != 3:
-                if function == 'is_tip':
-                    raise TypeError("{} must be a function that returns a list"
-                                    " of length *3* of ints or strings or "
-                                    "tuples of ints or strings")
-                raise TypeError("{} must be a function that returns a list"
-                                " of length *3* of floats or None")
-
-        def set_tip(tip, i, j, tip_types, ntips):
-            if str(tip) not in ntips:
-                ntips[str(tip)] = 0
-                tip_types[str(tip)] = []
-            ntips[str(tip)] += 1
-            tip_types[str(tip)].append((i, j))
-            return tip_types, ntips
-
-        n = self.nnodes
-        bc_types = np.zeros((n, self.degrees_freedom), dtype=np.intc)
-        bc_values = np.zeros((n, self.degrees_freedom), dtype=np.float64)
-        force_bc_types = np.zeros((n, self.degrees_freedom), dtype=np.intc)
-        force_bc_values = np.zeros((n, self.degrees_freedom),
-                                   dtype=np.float64)
-        tip_types = {}
-        num_force_bc_nodes = 0
-        ntips = {'model': n}
-        for i in range(n):
-            bnd = is_displacement_boundary(self.coords[i][:])
-            forces_bnd = is_force_boundary(self.coords[i][:])
-            tip = is_tip(self.coords[i][:])
-            is_force_node = 0
-            for j in range(self.degrees_freedom):
-                forces_bnd_j = forces_bnd[j]
-                bnd_j = bnd[j]
-                tip_j = tip[j]
-                if bnd_j is not None:
-                    bc_types[i, j] = np.intc(1)
-                    bc_values[i, j] = np.float64(bnd_j)
-                if forces_bnd_j is not None:
-                    is_force_node = 1
-                    force_bc_types[i, j] = np.intc(1)
-                    force_bc_values[i, j] = np.float64(
-                        forces_bnd_j / self.volume[i])
-                if tip_j is not None:
-                    if type(tip_j) is tuple:
-                        for tip_jk in tip_j:
-                            tip_types, ntips = set_tip(tip_jk, i, j,
-                                                       tip_types, ntips)
-                    else:
-                        tip_types, ntips = set_tip(tip_j, i, j, tip_types,
-                                                   ntips)
-            num_force_bc_nodes += is_force_node
-        if num_force_bc_nodes != 0:
-            force_bc_values = np.float64(
-                np.divide(force_bc_values, num_force_bc_nodes))
-        return (bc_types, bc_values, force_bc_types, force_bc_values,
-                tip_types, ntips)
+        """BC arrays and tips (:func:`boundary_conditions`)."""
+        return boundary_conditions(self.coords, self.volume,
+                                   is_displacement_boundary,
+                                   is_force_boundary, is_tip)
 
     # -------------------------------------------------------------- simulate
     def simulate(self, steps, u=None, ud=None, connectivity=None,
@@ -800,76 +809,36 @@ class Model(object):
         body_force = np.zeros((self.nnodes, 3), dtype=np.float64)
         damage = np.zeros(self.nnodes, dtype=np.float64)
         udd = np.zeros((self.nnodes, 3), dtype=np.float64)
-        if displacement_bc_magnitudes is None:
-            displacement_bc_magnitudes = np.zeros(first_step + steps - 1,
-                                                  dtype=np.float64)
-        elif type(displacement_bc_magnitudes) == np.ndarray:
-            if len(displacement_bc_magnitudes) < steps:
-                raise ValueError("displacement_bc_magnitudes length must be "
-                                 "equal to or greater than (first_step + steps"
-                                 " - 1), (expected {}, got {})".format(
-                                     first_step + steps - 1,
-                                     len(displacement_bc_magnitudes)))
-            displacement_bc_magnitudes = displacement_bc_magnitudes.astype(
-                np.float64)
-        else:
-            raise TypeError("displacement_bc_magnitudes type is wrong "
-                            "(expected {}, got {})".format(
-                                np.ndarray,
-                                type(displacement_bc_magnitudes)))
-        if force_bc_magnitudes is None:
-            force_bc_magnitudes = np.zeros(first_step + steps - 1,
-                                           dtype=np.float64)
-        elif type(force_bc_magnitudes) == np.ndarray:
-            if len(force_bc_magnitudes) < steps:
-                raise ValueError("force_bc_magnitudes length must be "
-                                 "equal to or greater than (first_step + steps"
-                                 " - 1), (expected {}, got {})".format(
-                                     first_step + steps - 1,
-                                     len(force_bc_magnitudes)))
-            force_bc_magnitudes = force_bc_magnitudes.astype(np.float64)
-        else:
-            raise TypeError("force_bc_magnitudes type is wrong "
-                            "(expected {}, got {})".format(
-                                np.ndarray, type(force_bc_magnitudes)))
+        displacement_bc_magnitudes = _schedule(
+            "displacement_bc_magnitudes", displacement_bc_magnitudes,
+            first_step, steps)
+        force_bc_magnitudes = _schedule("force_bc_magnitudes",
+                                        force_bc_magnitudes, first_step,
+                                        steps)
         if connectivity is None:
-            nlist, n_neigh = self.initial_connectivity
-            nlist = nlist.copy()
-            n_neigh = n_neigh.copy()
-        elif type(connectivity) == tuple:
-            if len(connectivity) != 2:
-                raise ValueError("connectivity size is wrong (expected 2,"
-                                 " got {})".format(len(connectivity)))
-            nlist, n_neigh = connectivity
+            nlist, n_neigh = (a.copy() for a in self.initial_connectivity)
         else:
-            raise TypeError("connectivity type is wrong (expected {} or"
-                            " {}, got {})".format(tuple, type(None),
-                                                  type(connectivity)))
+            nlist, n_neigh = _connectivity_pair(connectivity)
+        shape = (self.nnodes, self.max_neighbours)
         if regimes is None:
-            regimes = np.zeros((self.nnodes, self.max_neighbours),
-                               dtype=np.intc)
-        elif type(regimes) == np.ndarray:
-            if np.shape(regimes) != (self.nnodes, self.max_neighbours):
-                raise ValueError("regimes shape is wrong, and must be "
-                                 "(nnodes, max_neighbours) "
-                                 "(expected {}, got {})".format(
-                                     (self.nnodes, self.max_neighbours),
-                                     np.shape(regimes)))
-            regimes = regimes.astype(np.intc)
+            regimes = np.zeros(shape, dtype=np.intc)
+        elif type(regimes) != np.ndarray:
+            raise TypeError("regimes type is wrong (expected {} or {}, got "
+                            "{})".format(np.ndarray, type(None),
+                                         type(regimes)))
+        elif np.shape(regimes) != shape:
+            raise ValueError("regimes shape is wrong, and must be (nnodes, "
+                             "max_neighbours) (expected {}, got {})".format(
+                                 shape, np.shape(regimes)))
         else:
-            raise TypeError("regimes type is wrong "
-                            "(expected {} or {}, got {})".format(
-                                np.ndarray, type(None), type(regimes)))
-        if (bond_stiffness is None) and (critical_stretch is None):
-            bond_stiffness = self.bond_stiffness
-            critical_stretch = self.critical_stretch
-            plus_cs = self.plus_cs
-            nbond_types = self.nbond_types
-            nregimes = self.nregimes
+            regimes = regimes.astype(np.intc)
+        if bond_stiffness is None and critical_stretch is None:
+            (bond_stiffness, critical_stretch, plus_cs, nbond_types,
+             nregimes) = (self.bond_stiffness, self.critical_stretch,
+                          self.plus_cs, self.nbond_types, self.nregimes)
         else:
             (bond_stiffness, critical_stretch, plus_cs, nbond_types,
-             nregimes) = self._set_damage_model(bond_stiffness,
-                                                critical_stretch)
+             nregimes) = damage_model(bond_stiffness, critical_stretch)
             if nbond_types != self.nbond_types:
                 raise ValueError(
                     "Number of bond types has unexpectedly changed from when "

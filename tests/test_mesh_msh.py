@@ -57,3 +57,85 @@ def test_rejects_unsupported_files(tmp_path):
     p.write_text(MSH.replace("3 2 2 1 5 10 20 50", "3 2 2 1 5 10 20 60"))
     with pytest.raises((MeshFormatError, IndexError)):
         read_msh(p)
+
+
+# ------------------------------------------------- the reference's meshes
+def _reference_data():
+    """The reference checkout's test data and example meshes, where the
+    checkout is present (read-only; the build container)."""
+    from oracle.build_ref import DEFAULT_REFERENCE
+    root = DEFAULT_REFERENCE
+    if not (root / "peripy" / "test" / "data").is_dir():
+        pytest.skip("the reference checkout is not present")
+    return root
+
+
+def _count_msh(path):
+    """Node count and element counts by Gmsh type code, read from the file
+    with a separate minimal scan (the header counts and each element
+    line's second field), to check the reader against."""
+    lines = path.read_text().splitlines()
+    i = lines.index("$Nodes")
+    nnodes = int(lines[i + 1])
+    first = [float(v) for v in lines[i + 2].split()[1:4]]
+    j = lines.index("$Elements")
+    nel = int(lines[j + 1])
+    types = {}
+    for line in lines[j + 2:j + 2 + nel]:
+        code = int(line.split()[1])
+        types[code] = types.get(code, 0) + 1
+    return nnodes, first, types
+
+
+#: Gmsh element type codes and the cell names of the reader.
+_GMSH = {15: "vertex", 1: "line", 2: "triangle", 4: "tetra", 3: "quad"}
+
+
+@pytest.mark.parametrize("name", [
+    "peripy/test/data/example_mesh_transfinite.msh",
+    "peripy/test/data/example_mesh_large.msh",
+    "examples/example2/1650beam13539.msh"])
+def test_reads_the_reference_meshes(name):
+    """Every node and every element of the reference's own MSH meshes."""
+    path = _reference_data() / name
+    nnodes, first, types = _count_msh(path)
+    mesh = read_msh(path)
+    assert mesh.points.shape == (nnodes, 3)
+    assert np.array_equal(mesh.points[0], first)
+    for code, count in types.items():
+        assert mesh.cells_dict[_GMSH[code]].shape[0] == count
+    if name.endswith("1650beam13539.msh"):
+        assert nnodes == 13539
+
+
+def test_transfinite_model_as_the_reference_expects():
+    """``Model`` on ``example_mesh_transfinite.msh`` with transfinite=1 and
+    volume_total=1.0, the fixture of ``peripy/test/test_model.py:93-104``:
+    2116 nodes, node 69 at (0, 0.4888888888888889, 0) (test_model.py:195-201)
+    and every volume 1/2116 (test_model.py:271-274)."""
+    import probabilistic_peridynamics_gb300 as pp
+    from tests.test_model_host import HostIntegrator
+    path = _reference_data() / "peripy/test/data/example_mesh_transfinite.msh"
+
+    def displacement_boundary(x):
+        return [None, None, None]
+
+    model = pp.Model(path, integrator=HostIntegrator(), horizon=0.1,
+                     critical_stretch=0.05,
+                     bond_stiffness=18.0 * 0.05 / (np.pi * 0.1 ** 4),
+                     is_displacement_boundary=displacement_boundary,
+                     transfinite=1, volume_total=1.0)
+    assert model.coords.shape == (2116, 3) and model.nnodes == 2116
+    assert np.allclose(model.coords[69], [0, 0.4888888888888889, 0])
+    assert np.allclose(model.volume, np.ones(2116) / 2116.0)
+
+
+def test_large_mesh_warns_as_the_reference_expects():
+    """``example_mesh_large.msh`` through ``Model`` warns that the set-up
+    may take a while (``peripy/test/test_model.py:445-453``)."""
+    import probabilistic_peridynamics_gb300 as pp
+    from tests.test_model_host import HostIntegrator
+    path = _reference_data() / "peripy/test/data/example_mesh_large.msh"
+    with pytest.warns(UserWarning, match="this may take a while"):
+        pp.Model(path, integrator=HostIntegrator(), horizon=0.1,
+                 critical_stretch=1.0, bond_stiffness=1.0)
