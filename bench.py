@@ -82,6 +82,8 @@ def parse_args():
                    help="timed steps of each FP64 variant")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-variants", action="store_true",
+                   help="skip the batched, composite and adjoint timings")
     p.add_argument("--accuracy-steps", type=int, default=E2E_STEPS)
     p.add_argument("--workload",
                    choices=["large", "batched", "composite", "adjoint",
@@ -524,6 +526,128 @@ def time_fracture(w, steps, torch, ctx=None, settle=100):
             "bonds_broken_before": initial - int(np.sum(before[6] != -1)),
             "bonds_broken_after": initial - int(np.sum(after[6] != -1)),
             "eps0": FRACTURE_EPS0}
+
+
+def _kernel_name(integ):
+    return "k_tiled" if getattr(integ, "tiling", None) is not None \
+        else "k_mixed"
+
+
+def _roofline_frac(alg_bytes, kernel_ms, peak):
+    return alg_bytes / (kernel_ms * 1e-3) / 1e9 / peak
+
+
+def variant_batched(torch, peak, steps=20, warmup=3):
+    """The batched UQ form, briefly: 64 uneven instances (nx, ny uniform in
+    60..200, nz 5), Euler-Cromer, lognormal s0, U(0.9, 1.1) bond noise,
+    one persistent launch per step (graph replays), autotuned layout and
+    tile shape.  Algorithmic bytes: 4 B neighbour index + 8 B binary64
+    stiffness correction per bond, 336 B per node."""
+    import probabilistic_peridynamics_gb300 as pp
+    from probabilistic_peridynamics_gb300 import batch, lattice
+    t0 = time.perf_counter()
+    inst = batch.uq_instances(count=64, seed=2024, dx=DX)
+    b = batch.concatenate(inst)
+    k = lattice.bond_stiffness_pmb(BULK_MODULUS, HORIZON_CELLS * DX)
+    integ = pp.EulerCromerCUDA(DAMPING, dt=DT, precision="mixed")
+    sim = batch.BatchedSimulation(b, integ, k)
+    setup_s = time.perf_counter() - t0
+    ms = time_steps(integ, steps, warmup, torch) / steps
+    kernel_ms = time_kernel_launches(integ, 20, torch)
+    alg = b.bonds * (4 + 8) + b.nnodes * B_NODE_VV
+    out = {"bond_updates_per_s": b.bonds / (ms * 1e-3), "ms_per_step": ms,
+           "kernel_ms": kernel_ms, "kernel": _kernel_name(integ),
+           "algorithmic_bytes_per_launch": alg,
+           "roofline_frac": _roofline_frac(alg, kernel_ms, peak),
+           "nodes": b.nnodes, "bonds": b.bonds, "instances": len(inst),
+           "timed_steps": steps, "setup_s": setup_s,
+           "autotune_ms": integ.tuning}
+    del integ, sim
+    torch.cuda.empty_cache()
+    return out
+
+
+def variant_composite(torch, peak, ctx, steps=20, warmup=3):
+    """The irregular composite, briefly: 1M Poisson-disk points, three bond
+    types, trilinear damage, Velocity-Verlet, compensated force sums, faces
+    pulled COMPOSITE_RATE per step.  Algorithmic bytes: neighbour index,
+    bond type and regime (4 B each) per bond, 336 B per node."""
+    import probabilistic_peridynamics_gb300 as pp
+    from probabilistic_peridynamics_gb300.pointset import composite
+    t0 = time.perf_counter()
+    w = composite(context=ctx)
+    setup_s = time.perf_counter() - t0
+    n = w["coords"].shape[0]
+    bonds = int(w["family"].sum())
+    integ = pp.VelocityVerletCUDA(DAMPING, dt=DT, precision="mixed",
+                                  compensated=True, context=ctx)
+    integ.build(n, 3, w["max_neigh"], w["coords"], w["volume"], w["family"],
+                w["bc_types"], w["bc_values"], np.zeros((n, 3), dtype=np.intc),
+                np.zeros((n, 3)), None, w["bond_types"], w["densities"])
+    z = np.zeros((n, 3))
+    integ.create_buffers(w["nlist"], w["n_neigh"], w["bond_stiffness"],
+                         w["critical_stretch"], w["plus_cs"], z, z, z, z, z,
+                         np.zeros(n), None, w["nregimes"], w["nbond_types"])
+    ms = time_steps(integ, steps, warmup, torch, rate=COMPOSITE_RATE) / steps
+    kernel_ms = time_kernel_launches(integ, 50, torch, rate=COMPOSITE_RATE)
+    alg = bonds * (4 + 4 + 4) + n * B_NODE_VV
+    out = {"bond_updates_per_s": bonds / (ms * 1e-3), "ms_per_step": ms,
+           "kernel_ms": kernel_ms, "kernel": _kernel_name(integ),
+           "algorithmic_bytes_per_launch": alg,
+           "roofline_frac": _roofline_frac(alg, kernel_ms, peak),
+           "nodes": n, "bonds": bonds, "max_neigh": w["max_neigh"],
+           "timed_steps": steps, "setup_s": setup_s,
+           "autotune_ms": integ.tuning}
+    del integ
+    torch.cuda.empty_cache()
+    return out
+
+
+def variant_adjoint(torch, passes=2, warmup=1):
+    """One forward + checkpointed backward pass of the adjoint rollout
+    (50x50x5 lattice, 500 binary64 Euler steps, checkpoint every 50, 100
+    probe nodes); bond-updates count the forward, recomputed forward and
+    reverse steps."""
+    from probabilistic_peridynamics_gb300 import lattice
+    from probabilistic_peridynamics_gb300.adjoint import (AdjointProblem,
+                                                          rollout)
+    nx, ny, nz, steps, every = 50, 50, 5, 500, 50
+    coords = lattice.lattice_coords(nx, ny, nz, 1.0)
+    family, nlist, _ = lattice.lattice_family(nx, ny, nz, HORIZON_CELLS)
+    bc_types, bc_values = lattice.face_bcs(coords, 0)
+    n = coords.shape[0]
+    prob = AdjointProblem(coords, np.ones(n), nlist, bc_types, bc_values,
+                          1e-9 * np.arange(1, steps + 1), 0.5)
+    rng = np.random.default_rng(4)
+    probes = torch.tensor(rng.choice(n, 100, replace=False), device="cuda")
+    k0 = np.where(nlist != -1, 0.01 * rng.uniform(0.9, 1.1, nlist.shape),
+                  0.0)
+    k = torch.tensor(k0, dtype=torch.float32, device="cuda",
+                     requires_grad=True)
+
+    def one():
+        k.grad = None
+        u = rollout(k, 1.0, prob, steps, every)
+        (u[probes] ** 2).sum().backward()
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(passes):
+        one()
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / passes
+    bonds = int(family.sum())
+    del prob, k
+    torch.cuda.empty_cache()
+    return {"ms_per_pass": ms, "passes_per_s": 1e3 / ms,
+            "bond_updates_per_s": bonds * steps * 3 / (ms * 1e-3),
+            "nodes": n, "bonds": bonds, "steps": steps,
+            "checkpoint_every": every, "arithmetic": "binary64"}
 
 
 def e2e_simulate(w, torch):
@@ -1293,6 +1417,8 @@ def main():
     clk = clocks.stop()
     tuning = integ.tuning
     variant = int(integ._fargs.variant)
+    kernel = "k_tiled" if integ.tiling is not None else "k_mixed"
+    tiling_stats = integ.tiling.stats() if integ.tiling is not None else None
     launches = args.steps + (args.steps // 16 + 1
                              if args.steps >= 32 else 0)
     del integ
@@ -1312,7 +1438,8 @@ def main():
                                 "ms_per_step": ms_per_step,
                                 "kernel_ms": kernel_ms,
                                 "autotune_ms": tuning,
-                                "variant": variant}}
+                                "variant": variant, "kernel": kernel,
+                                "tiling": tiling_stats}}
     for name, precision, fused in (("plain_fp64", "float64", False),
                                    ("fused_fp64", "float64", True)):
         it = make_integrator(w, precision, fused, context=ctx)
@@ -1330,6 +1457,10 @@ def main():
                                                      torch)
 
     variants["fused_mixed_fracture"] = time_fracture(w, 20, torch, ctx)
+    if not args.no_variants:
+        variants["batched_uq"] = variant_batched(torch, peak)
+        variants["composite"] = variant_composite(torch, peak, ctx)
+        variants["adjoint"] = variant_adjoint(torch)
     acc = accuracy(w, args.accuracy_steps, torch) if args.accuracy_steps \
         else None
     acc_fracture = accuracy_fracture(w, torch)
@@ -1355,7 +1486,7 @@ def main():
                      "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "kernel": "k_mixed",
+                     "kernel": kernel,
                      "kernel_ms": kernel_ms,
                      "peak_source": ("measured" if peaks else "fallback")},
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,

@@ -100,12 +100,16 @@ __device__ __forceinline__ uint32_t load_u16x2(const uint8_t* p) {
 // (float(q - ref) h, exact) with the weight, then (kSuOffset) the
 // displacement halves with max|u|.  The bond vector xj - xi is exactly
 // h (q_j - q_i), as in k_mixed.
+//
+// srow: the tile's row offsets (units of 16 entries) relative to its first
+// row, which starts at entry tileE.
 template <int NW, int G, bool CORR, bool TYPES, bool COMP>
 __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tiling& t,
                                           const MixedConst& c, const Thresholds& th0,
                                           const Tables& tab, const unsigned char* __restrict__ dsm,
-                                          float4* __restrict__ sfrc, int parity, int tile,
-                                          int n0, int nt, int own0, int li, int lane) {
+                                          float4* __restrict__ sfrc, const int* __restrict__ srow,
+                                          int64_t tileE, int parity, int tile, int n0, int nt,
+                                          int own0, int li, int lane) {
     constexpr int GW = G / 2;  // words per batch
     const int sub = lane & 7;
     const bool node_ok = li < nt;
@@ -126,16 +130,10 @@ __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tilin
         th.lo = tab.tlo[inst];
         th.hi = tab.thi[inst];
     }
-    int np = 0;  // 32-bit words (pairs of entries) of this lane
-    int64_t rowE = 0;
-    if (node_ok) {
-        const int r0 = t.row_off[i];
-        np = t.row_off[i + 1] - r0;
-        rowE = 16 * (int64_t)r0;
-    }
+    const int np = node_ok ? srow[lic + 1] - srow[lic] : 0;  // words of this lane
     const int npw = __reduce_max_sync(kFull, np);
     // this lane's entry position of word m, half h: lp + 16 m + h
-    const int64_t lp = rowE + 2 * sub;
+    const int64_t lp = tileE + 16 * (int64_t)srow[lic] + 2 * sub;
     const uint32_t* ew = reinterpret_cast<const uint32_t*>(t.entry) + (lp >> 1);
     const uint32_t none = static_cast<uint32_t>(self) * 0x10001u;  // two own entries
     float sx = 0.f, sy = 0.f, sz = 0.f;
@@ -308,6 +306,7 @@ __global__ void __launch_bounds__(W * 32, MINB)
     float4* sp = reinterpret_cast<float4*>(dsm);
     float4* su = reinterpret_cast<float4*>(dsm + kSuOffset);
     __shared__ __align__(16) float4 sfrc[kTileNodes];
+    __shared__ int srow[kTileNodes + 1];
     __shared__ Tables tab;
     __shared__ int s_tile;
     const int lane = threadIdx.x & 31;
@@ -362,11 +361,17 @@ __global__ void __launch_bounds__(W * 32, MINB)
                 sp[h] = make_float4(fixed_diff(q.x, ref.x, c), fixed_diff(q.y, ref.y, c),
                                     fixed_diff(q.z, ref.z, c), __int_as_float(q.w));
             }
+            // row offsets of the tile, relative to its first row
+            const int rbase = t.row_off[n0];
+            for (int k = threadIdx.x; k <= nt; k += blockDim.x)
+                srow[k] = t.row_off[n0 + k] - rbase;
             cp_async_wait_all();
             __syncthreads();
+            const int64_t tileE = 16 * (int64_t)rbase;
             for (int base = warp * 4; base < nt; base += W * 4)  // warp-uniform
-                bond_tile<NW, kG, CORR, TYPES, COMP>(a, t, c, th0, tab, dsm, sfrc, parity, tile,
-                                                     n0, nt, own0, base + (lane >> 3), lane);
+                bond_tile<NW, kG, CORR, TYPES, COMP>(a, t, c, th0, tab, dsm, sfrc, srow, tileE,
+                                                     parity, tile, n0, nt, own0,
+                                                     base + (lane >> 3), lane);
             __syncthreads();
             for (int li = threadIdx.x >> 2; li < kTileNodes; li += blockDim.x >> 2)
                 node_phase(a, c, FrcView{sfrc}, m, parity, n0, li, n0 + nt);

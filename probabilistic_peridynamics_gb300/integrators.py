@@ -194,6 +194,7 @@ class _CUDAIntegrator(Integrator):
         # the tiled layout (False: the untiled kernel, from L1/L2)
         self.tiled = bool(tiled) and precision == "mixed"
         self.tiling = None
+        self.tile_target = 125  # nodes per brick of the internal order
         self._order = None
         self.tuning = None
         self.damping = 0.0
@@ -301,7 +302,7 @@ class _CUDAIntegrator(Integrator):
             from .tiling import brick_order
             self._order = brick_order(
                 self.coords, None if self._instances is None
-                else self._instances[0])
+                else self._instances[0], target=self.tile_target)
         self._build_special()
 
     def _check_densities(self):
@@ -431,6 +432,22 @@ class _CUDAIntegrator(Integrator):
                 from .autotune import tune_mixed
                 self.tuning = tune_mixed(self)
         self._create_special_buffers()
+
+    def _drop_tiling(self):
+        """Switch a mixed-precision integrator set up tiled to the untiled
+        kernel (the autotuner found it faster): repack the state in the
+        reference node order.  Only at create_buffers, before any step."""
+        torch = self._torch
+        n, mn = self.nnodes, self.max_neighbours
+        self.tiled = False
+        self.tiling = None
+        if self.stiffness_corrections_d is not None:
+            self.sc32_d = self._empty((n, mn), torch.float32)
+        a = self._fargs
+        a.tiling = None
+        a.sc32 = _ptr(self.sc32_d)
+        check(lib().pp_mixed_pack(ctypes.byref(a), self._parity,
+                                  self._stream), "pp_mixed_pack")
 
     def _create_mixed_buffers(self):
         torch = self._torch
