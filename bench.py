@@ -948,11 +948,11 @@ def load_peaks():
         return None
 
 
-def load_traffic():
-    """DRAM bytes per launch of the fused kernel from the committed ncu
-    summary (``profiles/*traffic*.txt``: a ``dram_bytes_per_launch N``
-    line)."""
-    for p in sorted((ROOT / "profiles").glob("*traffic*.txt")):
+def load_traffic(kernel):
+    """DRAM bytes per launch of ``kernel`` on the plate from the committed
+    ncu summary (``profiles/<kernel>_vv_200x200x10_traffic.txt``: a
+    ``dram_bytes_per_launch N`` line)."""
+    for p in sorted((ROOT / "profiles").glob(f"{kernel}_*traffic*.txt")):
         for line in p.read_text().splitlines():
             if line.startswith("dram_bytes_per_launch"):
                 try:
@@ -1414,7 +1414,13 @@ def main():
     ms_per_step = ms / args.steps
     value = job_throughput(world, w["bonds"], args.steps, ms)
     kernel_ms = time_kernel_launches(integ, 200, torch)
+    # about a second more of the same steps under the sampler, so that the
+    # clocks are seen under sustained load (not timed)
+    burst = max(1, int(1000.0 / max(ms_per_step, 1e-3)))
+    time_steps(integ, burst, 0, torch)
     clk = clocks.stop()
+    clk["window"] = ("warm-up, timed steps, 200 timed launches and "
+                     f"{burst} further steps (untimed)")
     tuning = integ.tuning
     variant = int(integ._fargs.variant)
     kernel = "k_tiled" if integ.tiling is not None else "k_mixed"
@@ -1432,7 +1438,7 @@ def main():
     peak = float(peaks["hbm_gbs"]) if peaks else 6800.0
     alg_bytes = w["bonds"] * B_BOND + w["nnodes"] * B_NODE_VV
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
-    traffic = load_traffic()
+    traffic = load_traffic(kernel)
 
     variants = {"fused_mixed": {"bond_updates_per_s": value,
                                 "ms_per_step": ms_per_step,
