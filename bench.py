@@ -99,7 +99,7 @@ def parse_args():
                         "setup: neighbour families and initial crack of the "
                         "plate, GPU against host and the reference")
     p.add_argument("--profile", choices=["mixed", "fp64", "plain",
-                                         "composite"],
+                                         "composite", "batched"],
                    help="only run 3 warm-up and 3 profiled launches of one "
                         "step variant on the full workload (for ncu)")
     return p.parse_args()
@@ -110,6 +110,9 @@ def profile_case(which):
     import torch
     if which == "composite":
         profile_composite()
+        return
+    if which == "batched":
+        profile_batched()
         return
     w = build_workload()
     precision = "mixed" if which == "mixed" else "float64"
@@ -164,6 +167,31 @@ def profile_composite():
     integ.context.stream.synchronize()
     torch.cuda.synchronize()
     print("profile case composite: 6 steps done", flush=True)
+
+
+def profile_batched():
+    """3 warm-up + 3 launches of the batched UQ step on 16 of the 64
+    instances (the same generator: nx, ny uniform in 60..200, nz 5; about
+    1.4M nodes, a few GB on the device), tiled layout, tile shape
+    PP_PROFILE_VARIANT (default 0, the one the autotuner picks for the 64
+    instances); no tuning launches."""
+    import torch
+    import probabilistic_peridynamics_gb300 as pp
+    from probabilistic_peridynamics_gb300 import batch, lattice
+    b = batch.concatenate(batch.uq_instances(count=16, seed=2024, dx=DX))
+    k = lattice.bond_stiffness_pmb(BULK_MODULUS, HORIZON_CELLS * DX)
+    integ = pp.EulerCromerCUDA(DAMPING, dt=DT, precision="mixed",
+                               autotune=False)
+    sim = batch.BatchedSimulation(b, integ, k)
+    integ._fargs.variant = int(os.environ.get("PP_PROFILE_VARIANT", "0"))
+    for s in range(6):
+        integ(PULL_RATE * (s + 1), 0.0)
+    integ.context.stream.synchronize()
+    torch.cuda.synchronize()
+    kernel = "k_tiled" if integ.tiling is not None else "k_mixed"
+    print(f"profile case batched: 6 steps done ({b.nnodes} nodes, {b.bonds}"
+          f" bonds, {kernel}, variant {integ._fargs.variant})", flush=True)
+    del sim
 
 
 # ----------------------------------------------------------------- workload
