@@ -565,6 +565,18 @@ def _roofline_frac(alg_bytes, kernel_ms, peak):
     return alg_bytes / (kernel_ms * 1e-3) / 1e9 / peak
 
 
+def _tuning_summary(tuning):
+    """The autotuner's choice against the untuned default (the tiled
+    layout's tile shape 0), from its per-candidate timings."""
+    if not tuning:
+        return None
+    best = min(tuning, key=tuning.get)
+    default = "tiled/0" if "tiled/0" in tuning else "untiled/0"
+    return {"chosen": best, "chosen_ms": tuning[best], "default": default,
+            "default_ms": tuning[default],
+            "speedup": tuning[default] / tuning[best]}
+
+
 def variant_batched(torch, peak, steps=20, warmup=3):
     """The batched UQ form, briefly: 64 uneven instances (nx, ny uniform in
     60..200, nz 5), Euler-Cromer, lognormal s0, U(0.9, 1.1) bond noise,
@@ -589,7 +601,8 @@ def variant_batched(torch, peak, steps=20, warmup=3):
            "roofline_frac": _roofline_frac(alg, kernel_ms, peak),
            "nodes": b.nnodes, "bonds": b.bonds, "instances": len(inst),
            "timed_steps": steps, "setup_s": setup_s,
-           "autotune_ms": integ.tuning}
+           "autotune_ms": integ.tuning,
+           "tuned_vs_default": _tuning_summary(integ.tuning)}
     del integ, sim
     torch.cuda.empty_cache()
     return out
@@ -625,7 +638,8 @@ def variant_composite(torch, peak, ctx, steps=20, warmup=3):
            "roofline_frac": _roofline_frac(alg, kernel_ms, peak),
            "nodes": n, "bonds": bonds, "max_neigh": w["max_neigh"],
            "timed_steps": steps, "setup_s": setup_s,
-           "autotune_ms": integ.tuning}
+           "autotune_ms": integ.tuning,
+           "tuned_vs_default": _tuning_summary(integ.tuning)}
     del integ
     torch.cuda.empty_cache()
     return out
@@ -1472,6 +1486,7 @@ def main():
                                 "ms_per_step": ms_per_step,
                                 "kernel_ms": kernel_ms,
                                 "autotune_ms": tuning,
+                                "tuned_vs_default": _tuning_summary(tuning),
                                 "variant": variant, "kernel": kernel,
                                 "tiling": tiling_stats}}
     for name, precision, fused in (("plain_fp64", "float64", False),
