@@ -128,6 +128,47 @@ __device__ __forceinline__ Bond32 bond32_xi(float xx, float xy, float xz, const 
     return b;
 }
 
+// bond32_xi of two bonds (a, b) of node i at once, on the paired FP32
+// instructions of sm_100 and later (__fadd2_rn, __fmul2_rn, __ffma2_rn: per
+// component the same IEEE round-to-nearest operation as the scalar one).
+// Every component goes through the operations of bond32_xi in the same order,
+// so half h is bit for bit bond32_xi of bond h; the approximate rsqrt and
+// division stay scalar calls of the same intrinsics.
+struct Bond32x2 {
+    float2 px, py, pz, s, ry, rxi;
+    __device__ __forceinline__ Bond32 half(int h) const {
+        Bond32 b;
+        b.px = h ? px.y : px.x;
+        b.py = h ? py.y : py.x;
+        b.pz = h ? pz.y : pz.x;
+        b.s = h ? s.y : s.x;
+        b.ry = h ? ry.y : ry.x;
+        b.rxi = h ? rxi.y : rxi.x;
+        return b;
+    }
+};
+
+__device__ __forceinline__ Bond32x2 bond32_xi2(float2 xx, float2 xy, float2 xz, const float4& ui,
+                                               const float4& uja, const float4& ujb) {
+    const float2 ex = make_float2(uja.x - ui.x, ujb.x - ui.x);
+    const float2 ey = make_float2(uja.y - ui.y, ujb.y - ui.y);
+    const float2 ez = make_float2(uja.z - ui.z, ujb.z - ui.z);
+    Bond32x2 b;
+    b.px = __fadd2_rn(xx, ex);
+    b.py = __fadd2_rn(xy, ey);
+    b.pz = __fadd2_rn(xz, ez);
+    const float2 mx = __fadd2_rn(b.px, xx), my = __fadd2_rn(b.py, xy), mz = __fadd2_rn(b.pz, xz);
+    const float2 xi2 = __ffma2_rn(xx, xx, __ffma2_rn(xy, xy, __fmul2_rn(xz, xz)));
+    const float2 y2 = __ffma2_rn(b.px, b.px, __ffma2_rn(b.py, b.py, __fmul2_rn(b.pz, b.pz)));
+    const float2 num = __ffma2_rn(ex, mx, __ffma2_rn(ey, my, __fmul2_rn(ez, mz)));
+    b.rxi = make_float2(rsqrtf(xi2.x), rsqrtf(xi2.y));
+    b.ry = make_float2(rsqrtf(y2.x), rsqrtf(y2.y));
+    const float2 lsum = __ffma2_rn(y2, b.ry, __fmul2_rn(xi2, b.rxi));
+    const float2 t = __fmul2_rn(num, b.rxi);
+    b.s = make_float2(__fdividef(t.x, lsum.x), __fdividef(t.y, lsum.y));
+    return b;
+}
+
 // The same from the fixed-point positions: xi = h (q_j - q_i), exact.
 __device__ __forceinline__ Bond32 bond32(const int4& qi, const float4& ui, const int4& qj,
                                          const float4& uj, const MixedConst& c) {
@@ -685,19 +726,37 @@ __device__ __forceinline__ void bond_phase_group(const pp_fused_args& a, const M
         reinterpret_cast<float*>(&sh.frc[li])[sub >> 1] = v;
 }
 
-// Node phase of one chunk: thread (node, component) updates one DOF of
-// node node0 + li; nodes at iend and beyond only join the warp's shuffles.
-template <class Shared>
-__device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedConst& c,
-                                           const Shared& sh, const StepMags& m, int parity,
-                                           int node0, int li, int iend) {
-    const int comp = threadIdx.x & 3;
-    const int i = node0 + li;
-    const bool active = i < iend;
-    const float4 fr = sh.frc[li];
+// The step's inputs of DOF `comp` of node i, read from the global arrays
+// (each only where node_update needs it).
+struct GlobalDof {
+    const pp_fused_args& a;
+    int parity;
+    int64_t i;
+    int comp;
+    __device__ __forceinline__ int flags() const { return a.nflags[i]; }
+    __device__ __forceinline__ float u_hi() const { return a.rec[parity][8 * i + 4 + comp]; }
+    __device__ __forceinline__ float u_lo() const { return a.ulo[parity][4 * i + comp]; }
+    __device__ __forceinline__ float v_hi() const { return a.vel[8 * i + comp]; }
+    __device__ __forceinline__ float v_lo() const { return a.vel[8 * i + 4 + comp]; }
+    __device__ __forceinline__ float rinv() const { return a.rho32[4 * i + comp]; }
+    __device__ __forceinline__ float acc() const { return a.acc[4 * i + comp]; }
+    // record word `comp` (position or weight), copied to the next record
+    __device__ __forceinline__ float qword() const { return a.rec[parity][8 * i + comp]; }
+};
+
+// Update of DOF `comp` of node i (comp 3: the record's fourth word) from its
+// force component `fc` (comp 3: the intact-bond count) and the inputs that
+// `in` reads (GlobalDof or a staged copy).  The four components of a node
+// sit on lanes S apart (xor shuffles by S and 2S); lanes with `active` false
+// only join the warp's shuffles.  Returns the node's max |u| for the running
+// maximum (0 on inactive lanes).
+template <int S, class In>
+__device__ __forceinline__ float node_update(const pp_fused_args& a, const MixedConst& c,
+                                             const StepMags& m, int parity, int i, int comp,
+                                             bool active, float fc, const In& in) {
     const int64_t o4 = 4 * (int64_t)i + comp;
     const int64_t o3 = 3 * (int64_t)i + comp;
-    const int fl = active ? a.nflags[i] : 0;
+    const int fl = active ? in.flags() : 0;
     const bool dof = active && comp < 3;
     // Boundary conditions are binary64 (slow on GB300's FP64 pipe): taken
     // only by warps that hold a boundary DOF.
@@ -707,25 +766,25 @@ __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedCo
     const bool any_dbc = __any_sync(kFull, dbc);
     float hi_new = 0.f, lo_new = 0.f;
     if (dof) {
-        const float body = comp == 0 ? fr.x : (comp == 1 ? fr.y : fr.z);
+        const float body = fc;
         float frc = body;
         if (any_fbc && fbc) frc = (float)((double)body + m.force * a.fc_values[o3]);
-        df uu{a.rec[parity][8 * (int64_t)i + 4 + comp], a.ulo[parity][o4]};
+        df uu{in.u_hi(), in.u_lo()};
         const df dt{c.dt_hi, c.dt_lo};
         if (a.integrator == PP_EULER) {
             uu = df_add(uu, df_mul_f(dt, frc));
         } else {
             const df half{c.half_hi, c.half_lo};
             const int64_t o8 = 8 * (int64_t)i + comp;
-            df v{a.vel[o8], a.vel[o8 + 4]};
-            const float rinv = a.rho32[o4];  // 1 / density
+            df v{in.v_hi(), in.v_lo()};
+            const float rinv = in.rinv();  // 1 / density
             float acc;
             if (a.integrator == PP_EULER_CROMER) {
                 acc = (frc - c.damping * v.hi) * rinv;
                 v = df_add(v, df_mul_f(dt, acc));
                 uu = df_add(uu, df_mul(dt, v));
             } else {
-                const df v1 = df_add(v, df_mul_f(half, a.acc[o4]));
+                const df v1 = df_add(v, df_mul_f(half, in.acc()));
                 acc = (frc - c.damping * v1.hi) * rinv;
                 v = df_add(v1, df_mul_f(half, acc));
                 uu = df_add(uu, df_mul(dt, df_add(v, df_mul_f(half, acc))));
@@ -740,27 +799,47 @@ __device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedCo
         a.frc[8 * (int64_t)i + comp] = frc;
         a.frc[8 * (int64_t)i + 4 + comp] = body;
     }
-    // max |u| of the node (quad shuffle) for the next step's error bounds
+    // max |u| of the node (shuffles within its four lanes) for the next
+    // step's error bounds
     float um = fabsf(hi_new);
-    um = fmaxf(um, __shfl_xor_sync(kFull, um, 1));
-    um = fmaxf(um, __shfl_xor_sync(kFull, um, 2));
+    um = fmaxf(um, __shfl_xor_sync(kFull, um, S));
+    um = fmaxf(um, __shfl_xor_sync(kFull, um, 2 * S));
     um *= 1.0f + 1.2e-7f;
     if (active) {
         // the whole record: position word comp, displacement word 4 + comp
         const int64_t o8 = 8 * (int64_t)i + comp;
-        a.rec[parity ^ 1][o8] = a.rec[parity][o8];
+        a.rec[parity ^ 1][o8] = in.qword();
         if (comp < 3) {
             a.rec[parity ^ 1][o8 + 4] = hi_new;
             a.ulo[parity ^ 1][o4] = lo_new;
         } else {
             a.rec[parity ^ 1][o8 + 4] = um;
             a.ulo[parity ^ 1][o4] = 0.f;
-            a.n_neigh[i] = (int)fr.w;
+            a.n_neigh[i] = (int)fc;
         }
     }
-    // running max |u| over the whole model (non-negative floats order as ints)
-    const int wmax = __reduce_max_sync(kFull, active ? __float_as_int(um) : 0);
+    return active ? um : 0.f;
+}
+
+// Raise the running max |u| of the model to the warp's largest `um`
+// (non-negative floats order as ints).
+__device__ __forceinline__ void raise_umax(const pp_fused_args& a, float um) {
+    const int wmax = __reduce_max_sync(kFull, __float_as_int(um));
     if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(reinterpret_cast<int*>(a.umax), wmax);
+}
+
+// Node phase of one chunk: thread (node, component) updates one DOF of
+// node node0 + li; nodes at iend and beyond only join the warp's shuffles.
+template <class Shared>
+__device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedConst& c,
+                                           const Shared& sh, const StepMags& m, int parity,
+                                           int node0, int li, int iend) {
+    const int comp = threadIdx.x & 3;
+    const int i = node0 + li;
+    const float4 fr = sh.frc[li];
+    const float fc = comp == 0 ? fr.x : (comp == 1 ? fr.y : (comp == 2 ? fr.z : fr.w));
+    raise_umax(a, node_update<1>(a, c, m, parity, i, comp, i < iend, fc,
+                                 GlobalDof{a, parity, i, comp}));
 }
 
 // One CTA of W warps loops over chunks of 16*W consecutive nodes (chunks

@@ -7,8 +7,9 @@
 // (pp_mixed.cuh), with the neighbour records gathered from shared memory:
 //
 //  0. A persistent CTA takes tiles from a device counter (t.sched[0]; the
-//     last CTA to finish resets both counter words for the next launch:
-//     no CTA waits for another).
+//     next tile is fetched while the current one computes; the last CTA to
+//     finish resets both counter words for the next launch: no CTA waits
+//     for another).
 //  1. Staging: the records of the tile's halo (every node its bonds reach,
 //     ascending) go to shared memory as two arrays, so that eight lanes
 //     reading eight consecutive records hit eight different bank quads:
@@ -20,14 +21,20 @@
 //     its row entries 16 m + l and 16 m + 8 + l as one 32-bit word of two
 //     16-bit entries (the next words are loaded while a batch computes),
 //     gathers both records from shared memory and does the FP32 bond
-//     arithmetic of bond32_xi; a clearly intact bond is decided by one
-//     compare, every other one in the per-node slow path (own error band,
-//     else the binary64 stretch from the reference r0 and the exact
-//     double-float displacement, peridynamics.cl:65-91).  A break writes
-//     the node's own entry.  The four per-node sums are reduced over the
-//     eight lanes (4 shuffles) and parked in shared memory.
-//  3. Node phase: as k_mixed (double-float update, next records written
-//     with coalesced stores), for the tile's nodes.
+//     arithmetic of bond32_xi, two bonds per paired FP32 instruction
+//     (bond32_xi2); a clearly intact bond is decided by one compare, every
+//     other one in the per-node slow path (own error band, else the
+//     binary64 stretch from the reference r0 and the exact double-float
+//     displacement, peridynamics.cl:65-91).  A break writes the node's own
+//     entry.  The four per-node sums are reduced over the eight lanes (4
+//     shuffles).
+//  3. Node update, right after the bond phase of each warp's two groups of
+//     four nodes, by the lanes that hold the sums (every lane: the even
+//     lanes of each eight update a node of the first group, the odd lanes
+//     one of the second): the double-float update of k_mixed's node phase
+//     (node_update), so its loads wait while other warps compute bonds,
+//     with no barrier and no shared-memory round trip.  The running max |u|
+//     is raised once per warp when the CTA ends.
 //
 // Entries are byte offsets (16 x halo index) into the staged arrays, so a
 // gather is one shared load at an immediate offset; a broken bond or
@@ -46,6 +53,7 @@ using namespace mixed;
 
 constexpr int kTileNodes = PP_TILE_NODES_MAX;
 constexpr int kHaloCap = PP_TILE_HALO_MAX;  // staged records per CTA
+
 // dynamic shared memory: positions at byte 0, displacements at kSuOffset
 constexpr int kSuOffset = 16 * kHaloCap;
 constexpr size_t kDynSmem = 32 * static_cast<size_t>(kHaloCap);
@@ -54,11 +62,6 @@ struct Tables {
     float thr[kMaxTable], k[kMaxTable], c[kMaxTable];  // regime tables or
                                                         // instance thresholds
     float tlo[kMaxTable], thi[kMaxTable];              // thresholds of thr[]
-};
-
-// node_phase reads the parked sums as sh.frc[li]
-struct FrcView {
-    const float4* frc;
 };
 
 // Staged record at byte offset `off` (an entry) of the array at `base`.
@@ -90,11 +93,12 @@ __device__ __forceinline__ uint32_t load_u16x2(const uint8_t* p) {
 // Bond phase of one node (eight lanes, lane `lane & 7` of them): internal
 // node n0 + li of tile `tile`, its staged record at halo index own0 + li
 // (entry own0 + li times 16, which its broken bonds and padding hold).
-// Parks (force x, y, z, intact count) in sfrc[li].  li >= nt: no node; the
-// lanes only join the warp's shuffles.  NW: the most 32-bit entry words a
-// lane can have (max_neigh / 16); the loop over them is unrolled, so every
-// entry's bit and offset are constants, and stops at the warp's longest
-// row.  A batch takes G entries (G / 2 words).
+// Returns the node's sums reduced over the eight lanes: force x on lanes 0
+// and 1 of the eight, y on 2 and 3, z on 4 and 5, the intact count on 6 and
+// 7.  li >= nt: no node; the lanes only join the warp's shuffles.  NW: the
+// most 32-bit entry words a lane can have (max_neigh / 16); the loop over
+// them is unrolled, so every entry's bit and offset are constants, and
+// stops at the warp's longest row.  A batch takes G entries (G / 2 words).
 //
 // dsm: the staged positions relative to the tile's reference point
 // (float(q - ref) h, exact) with the weight, then (kSuOffset) the
@@ -104,12 +108,11 @@ __device__ __forceinline__ uint32_t load_u16x2(const uint8_t* p) {
 // srow: the tile's row offsets (units of 16 entries) relative to its first
 // row, which starts at entry tileE.
 template <int NW, int G, bool CORR, bool TYPES, bool COMP>
-__device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tiling& t,
-                                          const MixedConst& c, const Thresholds& th0,
-                                          const Tables& tab, const unsigned char* __restrict__ dsm,
-                                          float4* __restrict__ sfrc, const int* __restrict__ srow,
-                                          int64_t tileE, int parity, int tile, int n0, int nt,
-                                          int own0, int li, int lane) {
+__device__ __forceinline__ float bond_tile(const pp_fused_args& a, const pp_tiling& t,
+                                           const MixedConst& c, const Thresholds& th0,
+                                           const Tables& tab, const unsigned char* __restrict__ dsm,
+                                           const int* __restrict__ srow, int64_t tileE, int parity,
+                                           int tile, int n0, int nt, int own0, int li, int lane) {
     constexpr int GW = G / 2;  // words per batch
     const int sub = lane & 7;
     const bool node_ok = li < nt;
@@ -185,12 +188,20 @@ __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tilin
             xj[kk] = staged(dsm, e[kk]);
             uj[kk] = staged(dsm + kSuOffset, e[kk]);
         }
+        // the FP32 bond arithmetic of the batch, two bonds per instruction
+        Bond32x2 bp[G / 2];
+#pragma unroll
+        for (int q = 0; q < G / 2; ++q) {
+            const float4 &xa = xj[2 * q], &xb = xj[2 * q + 1];
+            bp[q] = bond32_xi2(make_float2(xa.x - xi.x, xb.x - xi.x),
+                               make_float2(xa.y - xi.y, xb.y - xi.y),
+                               make_float2(xa.z - xi.z, xb.z - xi.z), ui, uj[2 * q], uj[2 * q + 1]);
+        }
 #pragma unroll
         for (int kk = 0; kk < G; ++kk) {
             const int k = 2 * m0 + kk;  // word k >> 1, half k & 1
             const bool valid = e[kk] != self;
-            const Bond32 b =
-                bond32_xi(xj[kk].x - xi.x, xj[kk].y - xi.y, xj[kk].z - xi.z, ui, uj[kk]);
+            const Bond32 b = bp[kk >> 1].half(kk & 1);
             float wt = xj[kk].w;  // k*vol (PMB) or vol (types)
             if constexpr (!TYPES) {
                 // clearly intact below th.lo; every other bond is decided in
@@ -292,7 +303,7 @@ __device__ __forceinline__ void bond_tile(const pp_fused_args& a, const pp_tilin
         v = reduce4c_group<8>(sx, cx, sy, cy, sz, cz, cnt, lane);
     else
         v = reduce4_group<8>(sx, sy, sz, cnt, lane);
-    if (node_ok && (sub & 1) == 0) reinterpret_cast<float*>(&sfrc[li])[sub >> 1] = v;
+    return v;
 }
 
 // One persistent CTA of W warps takes tiles until none are left.
@@ -305,7 +316,6 @@ __global__ void __launch_bounds__(W * 32, MINB)
     extern __shared__ __align__(16) unsigned char dsm[];
     float4* sp = reinterpret_cast<float4*>(dsm);
     float4* su = reinterpret_cast<float4*>(dsm + kSuOffset);
-    __shared__ __align__(16) float4 sfrc[kTileNodes];
     __shared__ int srow[kTileNodes + 1];
     __shared__ Tables tab;
     __shared__ int s_tile;
@@ -340,6 +350,7 @@ __global__ void __launch_bounds__(W * 32, MINB)
     if (threadIdx.x == 0) s_tile = atomicAdd(t.sched, 1);
     __syncthreads();
     int tile = s_tile;
+    float um = 0.f;  // this thread's largest max |u| (node updates)
     while (tile < t.ntiles) {
         const int n0 = t.tile_start[tile];
         const int nt = t.tile_start[tile + 1] - n0;
@@ -367,22 +378,46 @@ __global__ void __launch_bounds__(W * 32, MINB)
                 srow[k] = t.row_off[n0 + k] - rbase;
             cp_async_wait_all();
             __syncthreads();
+            // the next tile, fetched while this one computes (read after the
+            // barrier that ends this tile; rewritten only after the next
+            // staging barrier)
+            if (threadIdx.x == 0) s_tile = atomicAdd(t.sched, 1);
             const int64_t tileE = 16 * (int64_t)rbase;
-            for (int base = warp * 4; base < nt; base += W * 4)  // warp-uniform
-                bond_tile<NW, kG, CORR, TYPES, COMP>(a, t, c, th0, tab, dsm, sfrc, srow, tileE,
-                                                     parity, tile, n0, nt, own0,
-                                                     base + (lane >> 3), lane);
-            __syncthreads();
-            for (int li = threadIdx.x >> 2; li < kTileNodes; li += blockDim.x >> 2)
-                node_phase(a, c, FrcView{sfrc}, m, parity, n0, li, n0 + nt);
-        } else if (threadIdx.x == 0) {
-            atomicExch(a.status, PP_STATUS_BAD_TILING);
+            // Two groups of four nodes per warp, then one node update of all
+            // eight with every lane: the even lanes of each eight update the
+            // first group's node, the odd lanes the second's (each lane holds
+            // component (lane & 7) / 2 of both sums).
+            for (int base = warp * 8; base < nt; base += W * 8) {  // warp-uniform
+                const int la = base + (lane >> 3), lb = la + 4;
+                float va = 0.f, vb = 0.f;
+#pragma unroll 1
+                for (int g = 0; g < 2; ++g) {  // one copy of the bond loop
+                    const float v = bond_tile<NW, kG, CORR, TYPES, COMP>(
+                        a, t, c, th0, tab, dsm, srow, tileE, parity, tile, n0, nt, own0,
+                        la + 4 * g, lane);
+                    if (g == 0)
+                        va = v;
+                    else
+                        vb = v;
+                }
+                const bool odd = lane & 1;
+                const int li = odd ? lb : la;
+                const int comp = (lane & 7) >> 1;
+                const int i = n0 + li;
+                um = fmaxf(um, node_update<2>(a, c, m, parity, i, comp, li < nt, odd ? vb : va,
+                                              GlobalDof{a, parity, i, comp}));
+            }
+        } else {
+            if (threadIdx.x == 0) {
+                atomicExch(a.status, PP_STATUS_BAD_TILING);
+                s_tile = atomicAdd(t.sched, 1);
+            }
         }
-        __syncthreads();
-        if (threadIdx.x == 0) s_tile = atomicAdd(t.sched, 1);
+        // every warp is done with the staged halo (and s_tile is set)
         __syncthreads();
         tile = s_tile;
     }
+    raise_umax(a, um);
     // the last CTA to finish leaves both counter words zero for the next
     // launch (every CTA has taken its last tile by then)
     if (threadIdx.x == 0) {
