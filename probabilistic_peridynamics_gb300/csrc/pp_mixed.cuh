@@ -830,16 +830,16 @@ __device__ __forceinline__ void raise_umax(const pp_fused_args& a, float um) {
 
 // Node phase of one chunk: thread (node, component) updates one DOF of
 // node node0 + li; nodes at iend and beyond only join the warp's shuffles.
+// Returns the node's max |u| (0 beyond iend).
 template <class Shared>
-__device__ __forceinline__ void node_phase(const pp_fused_args& a, const MixedConst& c,
-                                           const Shared& sh, const StepMags& m, int parity,
-                                           int node0, int li, int iend) {
+__device__ __forceinline__ float node_phase(const pp_fused_args& a, const MixedConst& c,
+                                            const Shared& sh, const StepMags& m, int parity,
+                                            int node0, int li, int iend) {
     const int comp = threadIdx.x & 3;
     const int i = node0 + li;
     const float4 fr = sh.frc[li];
     const float fc = comp == 0 ? fr.x : (comp == 1 ? fr.y : (comp == 2 ? fr.z : fr.w));
-    raise_umax(a, node_update<1>(a, c, m, parity, i, comp, i < iend, fc,
-                                 GlobalDof{a, parity, i, comp}));
+    return node_update<1>(a, c, m, parity, i, comp, i < iend, fc, GlobalDof{a, parity, i, comp});
 }
 
 // One CTA of W warps loops over chunks of 16*W consecutive nodes (chunks
@@ -883,6 +883,9 @@ __global__ void __launch_bounds__(W * 32, MINB)
     __syncthreads();
     const StepMags m = step_mags(l);
     const Thresholds th0 = thresholds(c.s0, c.s0_err, qb);
+    // this thread's largest max |u| (node phases), raised once per warp at
+    // the end
+    float um = 0.f;
     if constexpr (SL >= 2) {
         // kNPW consecutive nodes per warp, kLPN lanes each
         constexpr int kLPN = kLanesPerNode;
@@ -913,9 +916,10 @@ __global__ void __launch_bounds__(W * 32, MINB)
             }
             __syncthreads();
             for (int li = threadIdx.x >> 2; li < kChunk; li += blockDim.x >> 2)
-                node_phase(a, c, sh, m, parity, node0, li, a.nnodes);
+                um = fmaxf(um, node_phase(a, c, sh, m, parity, node0, li, a.nnodes));
             __syncthreads();
         }
+        raise_umax(a, um);
         return;
     }
     const bool has = SL > 1 || lane < L;
@@ -943,9 +947,10 @@ __global__ void __launch_bounds__(W * 32, MINB)
         }
         __syncthreads();
         for (int li = threadIdx.x >> 2; li < kChunk; li += blockDim.x >> 2)
-            node_phase(a, c, sh, m, parity, node0, li, a.nnodes);
+            um = fmaxf(um, node_phase(a, c, sh, m, parity, node0, li, a.nnodes));
         __syncthreads();
     }
+    raise_umax(a, um);
 }
 
 inline MixedConst mixed_const(const pp_fused_args& a) {

@@ -363,36 +363,52 @@ __global__ void __launch_bounds__(W * 32, MINB)
             const float* rec = a.rec[parity];
             const int4 ref = reinterpret_cast<const int4*>(t.tile_ref)[tile];
             // the displacement halves by cp.async; positions converted to
-            // floats relative to the tile's reference point on the way.  In
-            // chunks of kPer records per thread, the halo indices of a chunk
-            // are all loaded before its records: a chunk waits on two load
-            // latencies, not two per record.
-            constexpr int kPer = 3;
+            // floats relative to the tile's reference point on the way.
+            if constexpr (!CORR && !TYPES) {
+                // In chunks of kPer records per thread, the halo indices of
+                // a chunk all loaded before its records: a chunk waits on two
+                // load latencies, not two per record.  (The instances with
+                // corrections or bond types hold more state across the
+                // staging, and the chunk's registers cost them more than
+                // the latency saves: measured on the batched and composite
+                // forms.)
+                constexpr int kPer = 3;
 #pragma unroll 1
-            for (int h0 = 0; h0 < nh; h0 += kPer * W * 32) {
-                int idx[kPer];
+                for (int h0 = 0; h0 < nh; h0 += kPer * W * 32) {
+                    int idx[kPer];
 #pragma unroll
-                for (int r = 0; r < kPer; ++r) {
-                    const int h = h0 + threadIdx.x + r * W * 32;
-                    const int j = h < nh ? hl[h] : 0;
-                    idx[r] = static_cast<unsigned>(j) < static_cast<unsigned>(a.nnodes) ? j : 0;
-                }
-                int4 q[kPer];
+                    for (int r = 0; r < kPer; ++r) {
+                        const int h = h0 + threadIdx.x + r * W * 32;
+                        const int j = h < nh ? hl[h] : 0;
+                        idx[r] =
+                            static_cast<unsigned>(j) < static_cast<unsigned>(a.nnodes) ? j : 0;
+                    }
+                    int4 q[kPer];
 #pragma unroll
-                for (int r = 0; r < kPer; ++r) {
-                    const int h = h0 + threadIdx.x + r * W * 32;
-                    if (h < nh) {
-                        cp_async16(&su[h], rec + 8 * (int64_t)idx[r] + 4);
-                        q[r] = __ldg(reinterpret_cast<const int4*>(rec + 8 * (int64_t)idx[r]));
+                    for (int r = 0; r < kPer; ++r) {
+                        const int h = h0 + threadIdx.x + r * W * 32;
+                        if (h < nh) {
+                            cp_async16(&su[h], rec + 8 * (int64_t)idx[r] + 4);
+                            q[r] = __ldg(reinterpret_cast<const int4*>(rec + 8 * (int64_t)idx[r]));
+                        }
+                    }
+#pragma unroll
+                    for (int r = 0; r < kPer; ++r) {
+                        const int h = h0 + threadIdx.x + r * W * 32;
+                        if (h < nh)
+                            sp[h] = make_float4(
+                                fixed_diff(q[r].x, ref.x, c), fixed_diff(q[r].y, ref.y, c),
+                                fixed_diff(q[r].z, ref.z, c), __int_as_float(q[r].w));
                     }
                 }
-#pragma unroll
-                for (int r = 0; r < kPer; ++r) {
-                    const int h = h0 + threadIdx.x + r * W * 32;
-                    if (h < nh)
-                        sp[h] = make_float4(fixed_diff(q[r].x, ref.x, c),
-                                            fixed_diff(q[r].y, ref.y, c),
-                                            fixed_diff(q[r].z, ref.z, c), __int_as_float(q[r].w));
+            } else {
+                for (int h = threadIdx.x; h < nh; h += blockDim.x) {
+                    int idx = hl[h];
+                    idx = static_cast<unsigned>(idx) < static_cast<unsigned>(a.nnodes) ? idx : 0;
+                    cp_async16(&su[h], rec + 8 * (int64_t)idx + 4);
+                    const int4 q = __ldg(reinterpret_cast<const int4*>(rec + 8 * (int64_t)idx));
+                    sp[h] = make_float4(fixed_diff(q.x, ref.x, c), fixed_diff(q.y, ref.y, c),
+                                        fixed_diff(q.z, ref.z, c), __int_as_float(q.w));
                 }
             }
             // row offsets of the tile, relative to its first row
