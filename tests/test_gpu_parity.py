@@ -400,11 +400,14 @@ def test_row_widths(factor, width, mode):
 
 # ------------------------------------------------- force boundary conditions
 @pytest.mark.parametrize("kind", list(_KINDS))
-@pytest.mark.parametrize("mode", ["plain", "fused64", "mixed", "mixed_run"])
+@pytest.mark.parametrize("mode", ["plain", "fused64", "mixed", "mixed_run",
+                                  "mixed_untiled"])
 def test_force_boundary_conditions(kind, mode):
     """A force on the x-max face (F / vol / n_face per node, as
     ``_set_boundary_conditions`` spreads it, ``peripy/model.py:1194-1209``)
-    ramped over the steps, the x-min face clamped; bonds break under it."""
+    ramped over the steps, the x-min face clamped; bonds break under it.
+    The mixed step on both layouts (tiled: the node update runs in the bond
+    phase's lanes; untiled: in the node phase)."""
     import probabilistic_peridynamics_gb300 as pp
     setup = breaking_setup(kind)
     coords, vol = setup["coords"], setup["volume"]
@@ -425,10 +428,14 @@ def test_force_boundary_conditions(kind, mode):
     cls = getattr(pp, _KINDS[kind])
     kw = dict(fused=mode != "plain",
               precision="mixed" if mode.startswith("mixed") else "float64")
+    if mode.startswith("mixed"):
+        kw.update(tiled=mode != "mixed_untiled", autotune=False)
     integ = (cls(dt=setup["dt"], **kw) if kind == "euler"
              else cls(damping=0.5, dt=setup["dt"], **kw))
     out = run_integrator(integ, setup, steps, dmags, force_mags=fmags,
                          use_run=mode.endswith("_run"))
+    if mode.startswith("mixed"):
+        assert (integ.tiling is not None) == (mode != "mixed_untiled")
     ref = run_oracle(kind, setup, steps, dmags, force_mags=fmags,
                      damping=0.0 if kind == "euler" else 0.5)
     assert int((setup["nlist"] != -1).sum() - (ref[6] != -1).sum()) > 0
