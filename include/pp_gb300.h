@@ -216,7 +216,7 @@ int pp_update_displacement_velocity_verlet(
 /* ------------------------------------------------------------------------ */
 
 #define PP_TILE_NODES_MAX           128   /* internal nodes per tile       */
-#define PP_TILE_HALO_MAX            1536  /* largest halo_cap: 32 bytes of
+#define PP_TILE_HALO_MAX            768   /* largest halo_cap: 32 bytes of
                                              shared memory per record      */
 
 typedef struct pp_tiling {

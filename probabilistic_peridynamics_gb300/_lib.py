@@ -34,7 +34,7 @@ PP_STATUS_OK = 0
 PP_STATUS_COPY_TIMEOUT = 1
 PP_STATUS_BAD_TILING = 2
 PP_TILE_NODES_MAX = 128
-PP_TILE_HALO_MAX = 1536
+PP_TILE_HALO_MAX = 768
 
 _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32

@@ -54,15 +54,24 @@ using namespace mixed;
 constexpr int kTileNodes = PP_TILE_NODES_MAX;
 constexpr int kHaloCap = PP_TILE_HALO_MAX;  // staged records per CTA
 
-// dynamic shared memory: positions at byte 0, displacements at kSuOffset
+// dynamic shared memory: positions at byte 0, displacements at kSuOffset,
+// then (kTabOffset) the regime tables or instance thresholds, allocated
+// only for the launches that read them (bond types, batch instances)
 constexpr int kSuOffset = 16 * kHaloCap;
-constexpr size_t kDynSmem = 32 * static_cast<size_t>(kHaloCap);
+constexpr int kTabOffset = 32 * kHaloCap;
 
 struct Tables {
     float thr[kMaxTable], k[kMaxTable], c[kMaxTable];  // regime tables or
                                                         // instance thresholds
     float tlo[kMaxTable], thi[kMaxTable];              // thresholds of thr[]
 };
+
+// Dynamic shared memory of a launch: the halo arrays, plus the tables when
+// the step reads them.
+inline size_t dyn_smem(const pp_fused_args& a) {
+    const bool tables = a.bond_types != nullptr || a.node_instance != nullptr;
+    return static_cast<size_t>(kTabOffset) + (tables ? sizeof(Tables) : 0);
+}
 
 // Staged record at byte offset `off` (an entry) of the array at `base`.
 __device__ __forceinline__ float4 staged(const unsigned char* base, int off) {
@@ -317,7 +326,7 @@ __global__ void __launch_bounds__(W * 32, MINB)
     float4* sp = reinterpret_cast<float4*>(dsm);
     float4* su = reinterpret_cast<float4*>(dsm + kSuOffset);
     __shared__ int srow[kTileNodes + 1];
-    __shared__ Tables tab;
+    Tables& tab = *reinterpret_cast<Tables*>(dsm + kTabOffset);  // (when allocated)
     __shared__ int s_tile;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -474,21 +483,25 @@ template <int NW, bool CORR, bool TYPES, bool COMP, int W, int MINB>
 int launch_tiled_instance(const pp_fused_args& a, const pp_tiling& t, int parity, const Launch& l,
                           cudaStream_t st) {
     auto kernel = k_tiled<NW, CORR, TYPES, COMP, W, MINB>;
-    static int cached_grid = 0;
-    if (cached_grid == 0) {
+    // resident CTAs per SM: cached per kernel instance, with and without
+    // the tables in shared memory
+    static int cached_grid[2] = {0, 0};
+    const size_t dyn = dyn_smem(a);
+    int& cg = cached_grid[dyn > static_cast<size_t>(kTabOffset)];
+    if (cg == 0) {
         if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(kDynSmem)) != cudaSuccess)
+                                 static_cast<int>(kTabOffset + sizeof(Tables))) != cudaSuccess)
             return PP_ERROR_CUDA;
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, W * 32, kDynSmem) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, W * 32, dyn) !=
                 cudaSuccess ||
             per_sm < 1)
             return PP_ERROR_UNSUPPORTED;
-        cached_grid = per_sm * sm_count();
+        cg = per_sm * sm_count();
     }
-    const int grid = t.ntiles < cached_grid ? t.ntiles : cached_grid;
+    const int grid = t.ntiles < cg ? t.ntiles : cg;
     if (grid < 1) return PP_SUCCESS;
-    kernel<<<grid, W * 32, kDynSmem, st>>>(a, t, mixed_const(a), parity, l);
+    kernel<<<grid, W * 32, dyn, st>>>(a, t, mixed_const(a), parity, l);
     return launch_status();
 }
 

@@ -22,9 +22,10 @@ from . import _lib
 from ._lib import check, lib
 
 TILE_NODES_MAX = 128
-#: Halo capacity per tile: 32 bytes of shared memory per record, 48 KB per
-#: CTA, so that four CTAs of 256 threads fit on an SM.
-HALO_CAP = 1536
+#: Halo capacity per tile: 32 bytes of shared memory per record, 24 KB per
+#: CTA, so that eight CTAs of 128 threads fit on an SM (a tile whose halo is
+#: longer is split).
+HALO_CAP = 768
 
 
 def brick_order(coords, segments=None, target=125, max_nodes=TILE_NODES_MAX):

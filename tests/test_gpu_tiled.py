@@ -90,7 +90,7 @@ def test_plate_fracture_tiled_equals_untiled(plate):
         100_000
     st = got[2]
     assert st["tiles"] == 3200 and st["splits"] == 0
-    assert st["halo_max"] <= 1536
+    assert st["halo_max"] <= 768
     _same(got, ref)
 
 
