@@ -130,7 +130,7 @@ def profile_case(which):
         integ.create_buffers(w["nlist"], w["n_neigh"], w["k"], w["s0"], None,
                              z, z, z, z, z, np.zeros(w["nnodes"]), None, 1, 1)
         integ._fargs.variant = int(os.environ.get(
-            "PP_PROFILE_VARIANT", "0" if tiled else "1"))
+            "PP_PROFILE_VARIANT", "1"))
     else:
         integ = make_integrator(w, precision, which != "plain",
                                 autotune=False)
