@@ -129,10 +129,11 @@ def test_split_halos_and_random_order(monkeypatch):
     assert int(np.sum(w["nlist"] != -1) - np.sum(got[0][6] != -1)) > 0
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("compensated", [False, True])
-def test_composite_types_tiled_equals_untiled(compensated):
+def test_composite_types_tiled_equals_untiled(compensated, variant):
     """Bond types, three regimes, softening and breaking (2,500-point
-    composite, 200 steps)."""
+    composite, 200 steps), on every tile shape."""
     import probabilistic_peridynamics_gb300 as pp
     from probabilistic_peridynamics_gb300.pointset import composite
     w = composite(count=2500, box=(0.16, 0.08, 0.04), split=0.08, seed=2)
@@ -145,14 +146,15 @@ def test_composite_types_tiled_equals_untiled(compensated):
     ref = _run(cls, w, steps, mags, False, types=True,
                compensated=compensated)
     got = _run(cls, w, steps, mags, True, types=True,
-               compensated=compensated)
+               compensated=compensated, variant=variant)
     assert np.count_nonzero(got[1]) > 0
     _same(got, ref)
 
 
-def test_batched_instances_tiled_equals_untiled():
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_batched_instances_tiled_equals_untiled(variant):
     """Per-instance critical stretch and per-bond stiffness corrections
-    (five uneven lattices, Euler-Cromer, breaking)."""
+    (five uneven lattices, Euler-Cromer, breaking), on every tile shape."""
     import probabilistic_peridynamics_gb300 as pp
     from probabilistic_peridynamics_gb300 import batch
     inst = batch.uq_instances(count=5, seed=5, nx_range=(6, 10),
@@ -171,6 +173,6 @@ def test_batched_instances_tiled_equals_untiled():
     args = dict(instances=(b.node_instance, b.instance_s0),
                 corrections=b.stiffness_corrections)
     ref = _run(cls, w, steps, mags, False, **args)
-    got = _run(cls, w, steps, mags, True, **args)
+    got = _run(cls, w, steps, mags, True, variant=variant, **args)
     assert int(np.sum(b.nlist != -1) - np.sum(got[0][6] != -1)) > 0
     _same(got, ref)
