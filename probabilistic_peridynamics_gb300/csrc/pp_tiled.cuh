@@ -60,17 +60,21 @@ constexpr int kHaloCap = PP_TILE_HALO_MAX;  // staged records per CTA
 constexpr int kSuOffset = 16 * kHaloCap;
 constexpr int kTabOffset = 32 * kHaloCap;
 
-struct Tables {
-    float thr[kMaxTable], k[kMaxTable], c[kMaxTable];  // regime tables or
-                                                        // instance thresholds
-    float tlo[kMaxTable], thi[kMaxTable];              // thresholds of thr[]
+// One entry of the regime tables (bond types: index type * nregimes +
+// regime) or of the per-instance thresholds (batch instances): 32 bytes, so
+// that every field is at a fixed offset from the entry.
+struct TabEntry {
+    float thr, k, c;  // critical stretch (rounded to float), stiffness, plus_cs
+    float tlo, thi;   // thresholds of thr (clearly below / clearly above)
+    float pad[3];
 };
 
-// Dynamic shared memory of a launch: the halo arrays, plus the tables when
-// the step reads them.
+// Dynamic shared memory of a launch: the halo arrays, plus the table
+// entries the step reads (none for plain PMB).
 inline size_t dyn_smem(const pp_fused_args& a) {
-    const bool tables = a.bond_types != nullptr || a.node_instance != nullptr;
-    return static_cast<size_t>(kTabOffset) + (tables ? sizeof(Tables) : 0);
+    const int entries = a.bond_types ? a.nbond_types * a.nregimes
+                                     : (a.node_instance ? a.ninstances : 0);
+    return static_cast<size_t>(kTabOffset) + sizeof(TabEntry) * static_cast<size_t>(entries);
 }
 
 // Staged record at byte offset `off` (an entry) of the array at `base`.
@@ -119,7 +123,8 @@ __device__ __forceinline__ uint32_t load_u16x2(const uint8_t* p) {
 template <int NW, int G, bool CORR, bool TYPES, bool COMP>
 __device__ __forceinline__ float bond_tile(const pp_fused_args& a, const pp_tiling& t,
                                            const MixedConst& c, const Thresholds& th0,
-                                           const Tables& tab, const unsigned char* __restrict__ dsm,
+                                           const TabEntry* __restrict__ tab,
+                                           const unsigned char* __restrict__ dsm,
                                            const int* __restrict__ srow, int64_t tileE, int parity,
                                            int tile, int n0, int nt, int own0, int li, int lane) {
     constexpr int GW = G / 2;  // words per batch
@@ -136,11 +141,11 @@ __device__ __forceinline__ float bond_tile(const pp_fused_args& a, const pp_tili
     Thresholds th = th0;
     if (!TYPES && a.node_instance) {
         const int inst = a.node_instance[i];
-        s0f = tab.thr[inst];
+        s0f = tab[inst].thr;
         s0err = 6.0e-8f * fabsf(s0f);
         s0d = a.instance_s0[inst];
-        th.lo = tab.tlo[inst];
-        th.hi = tab.thi[inst];
+        th.lo = tab[inst].tlo;
+        th.hi = tab[inst].thi;
     }
     const int np = node_ok ? srow[lic + 1] - srow[lic] : 0;  // words of this lane
     const int npw = __reduce_max_sync(kFull, np);
@@ -229,9 +234,9 @@ __device__ __forceinline__ float bond_tile(const pp_fused_args& a, const pp_tili
                 if (!valid) continue;
                 bool ambiguous = false;
                 const int reg = next_regime(rg[kk], bt[kk], nr, [&](int idx) {
-                    if (b.s < tab.tlo[idx]) return true;
-                    if (b.s > tab.thi[idx]) return false;
-                    const float thr = tab.thr[idx];
+                    if (b.s < tab[idx].tlo) return true;
+                    if (b.s > tab[idx].thi) return false;
+                    const float thr = tab[idx].thr;
                     const float d = b.s - thr;
                     if (!(fabsf(d) > band32(ui, uj[kk], b, c) + 6.0e-8f * fabsf(thr)))
                         ambiguous = true;
@@ -247,7 +252,7 @@ __device__ __forceinline__ float bond_tile(const pp_fused_args& a, const pp_tili
                     t.entry[pos] = static_cast<uint16_t>(self);
                     continue;
                 }
-                wt *= fmaf(b.s, tab.k[bt[kk] + reg], tab.c[bt[kk] + reg]);
+                wt *= fmaf(b.s, tab[bt[kk] + reg].k, tab[bt[kk] + reg].c);
                 float fv = wt * b.ry;
                 if constexpr (CORR) fv *= sc[kk];
                 acc_mul<COMP>(sx, cx, fv, b.px);
@@ -293,7 +298,7 @@ __device__ __forceinline__ float bond_tile(const pp_fused_args& a, const pp_tili
                 });
                 if (reg != rgk) t.regime[pos] = static_cast<uint8_t>(reg);
                 intact = reg < nr;
-                if (intact) wt *= fmaf(b.s, tab.k[btk + reg], tab.c[btk + reg]);
+                if (intact) wt *= fmaf(b.s, tab[btk + reg].k, tab[btk + reg].c);
             }
             if (!intact) {
                 t.entry[pos] = static_cast<uint16_t>(self);
@@ -326,7 +331,7 @@ __global__ void __launch_bounds__(W * 32, MINB)
     float4* sp = reinterpret_cast<float4*>(dsm);
     float4* su = reinterpret_cast<float4*>(dsm + kSuOffset);
     __shared__ int srow[kTileNodes + 1];
-    Tables& tab = *reinterpret_cast<Tables*>(dsm + kTabOffset);  // (when allocated)
+    TabEntry* tab = reinterpret_cast<TabEntry*>(dsm + kTabOffset);  // (when allocated)
     __shared__ int s_tile;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -338,20 +343,20 @@ __global__ void __launch_bounds__(W * 32, MINB)
         for (int k = threadIdx.x; k < nt; k += blockDim.x) {
             const float thr = (float)a.critical_stretch_table[k];
             const Thresholds th = thresholds(thr, 6.0e-8f * fabsf(thr), qb);
-            tab.thr[k] = thr;
-            tab.tlo[k] = th.lo;
-            tab.thi[k] = th.hi;
-            tab.k[k] = (float)a.bond_stiffness_table[k];
-            tab.c[k] = (float)a.plus_cs[k];
+            tab[k].thr = thr;
+            tab[k].tlo = th.lo;
+            tab[k].thi = th.hi;
+            tab[k].k = (float)a.bond_stiffness_table[k];
+            tab[k].c = (float)a.plus_cs[k];
         }
     } else {
         if (a.node_instance)
             for (int k = threadIdx.x; k < a.ninstances; k += blockDim.x) {
                 const float thr = (float)a.instance_s0[k];
                 const Thresholds th = thresholds(thr, 6.0e-8f * fabsf(thr), qb);
-                tab.thr[k] = thr;
-                tab.tlo[k] = th.lo;
-                tab.thi[k] = th.hi;
+                tab[k].thr = thr;
+                tab[k].tlo = th.lo;
+                tab[k].thi = th.hi;
             }
     }
     const StepMags m = step_mags(l);
@@ -483,22 +488,25 @@ template <int NW, bool CORR, bool TYPES, bool COMP, int W, int MINB>
 int launch_tiled_instance(const pp_fused_args& a, const pp_tiling& t, int parity, const Launch& l,
                           cudaStream_t st) {
     auto kernel = k_tiled<NW, CORR, TYPES, COMP, W, MINB>;
-    // resident CTAs per SM: cached per kernel instance, with and without
-    // the tables in shared memory
-    static int cached_grid[2] = {0, 0};
+    // resident CTAs per SM: cached per kernel instance for the last
+    // dynamic shared-memory size (it varies with the table entries)
+    static size_t cached_dyn = 0;
+    static int cached_grid = 0;
     const size_t dyn = dyn_smem(a);
-    int& cg = cached_grid[dyn > static_cast<size_t>(kTabOffset)];
-    if (cg == 0) {
+    if (cached_grid == 0 || cached_dyn != dyn) {
         if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(kTabOffset + sizeof(Tables))) != cudaSuccess)
+                                 static_cast<int>(kTabOffset + sizeof(TabEntry) * kMaxTable)) !=
+            cudaSuccess)
             return PP_ERROR_CUDA;
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, W * 32, dyn) !=
                 cudaSuccess ||
             per_sm < 1)
             return PP_ERROR_UNSUPPORTED;
-        cg = per_sm * sm_count();
+        cached_grid = per_sm * sm_count();
+        cached_dyn = dyn;
     }
+    const int cg = cached_grid;
     const int grid = t.ntiles < cg ? t.ntiles : cg;
     if (grid < 1) return PP_SUCCESS;
     kernel<<<grid, W * 32, dyn, st>>>(a, t, mixed_const(a), parity, l);
