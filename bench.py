@@ -173,7 +173,7 @@ def profile_batched():
     """3 warm-up + 3 launches of the batched UQ step on 16 of the 64
     instances (the same generator: nx, ny uniform in 60..200, nz 5; about
     1.4M nodes, a few GB on the device), tiled layout, tile shape
-    PP_PROFILE_VARIANT (default 0, the one the autotuner picks for the 64
+    PP_PROFILE_VARIANT (default 1, the one the autotuner picks for the 64
     instances); no tuning launches."""
     import torch
     import probabilistic_peridynamics_gb300 as pp
@@ -183,7 +183,7 @@ def profile_batched():
     integ = pp.EulerCromerCUDA(DAMPING, dt=DT, precision="mixed",
                                autotune=False)
     sim = batch.BatchedSimulation(b, integ, k)
-    integ._fargs.variant = int(os.environ.get("PP_PROFILE_VARIANT", "0"))
+    integ._fargs.variant = int(os.environ.get("PP_PROFILE_VARIANT", "1"))
     for s in range(6):
         integ(PULL_RATE * (s + 1), 0.0)
     integ.context.stream.synchronize()
