@@ -39,9 +39,10 @@
 // Entries are byte offsets (16 x halo index) into the staged arrays, so a
 // gather is one shared load at an immediate offset; a broken bond or
 // padding holds the node's own entry.  Every count read from the tiling is
-// checked before it addresses shared memory: a tile with more than
-// PP_TILE_NODES_MAX nodes or a halo longer than PP_TILE_HALO_MAX is
-// skipped and reported in the status word (PP_STATUS_BAD_TILING).
+// checked before it addresses shared or global memory: a tile with more
+// than PP_TILE_NODES_MAX nodes or a halo longer than the tiling's halo_cap
+// (the set-up marks a tile to split with halo_cap + 1) is skipped and
+// reported in the status word (PP_STATUS_BAD_TILING).
 #pragma once
 
 #include "pp_mixed.cuh"
@@ -370,7 +371,9 @@ __global__ void __launch_bounds__(W * 32, MINB)
         const int nt = t.tile_start[tile + 1] - n0;
         const int nh = t.halo_count[tile];
         const int own0 = t.own_off[tile];
-        const bool ok = nt >= 0 && nt <= kTileNodes && nh >= 0 && nh <= kHaloCap &&
+        // (halo_cap <= kHaloCap is checked on the host; a halo count above
+        // halo_cap is also the set-up's mark of a tile to split)
+        const bool ok = nt >= 0 && nt <= kTileNodes && nh >= 0 && nh <= t.halo_cap &&
                         own0 >= 0 && own0 + nt <= nh && n0 >= 0 && n0 + nt <= a.nnodes;
         if (ok) {
             const int32_t* hl = t.halo + (int64_t)tile * t.halo_cap;

@@ -176,3 +176,41 @@ def test_batched_instances_tiled_equals_untiled(variant):
     got = _run(cls, w, steps, mags, True, variant=variant, **args)
     assert int(np.sum(b.nlist != -1) - np.sum(got[0][6] != -1)) > 0
     _same(got, ref)
+
+
+@pytest.mark.parametrize("field", ["halo_max", "split_mark", "tile_start"])
+def test_bad_tile_reported(field, monkeypatch):
+    """A tile whose counts exceed the kernel's limits (here set on the host
+    after the set-up: a halo longer than PP_TILE_HALO_MAX; the set-up's
+    mark of a tile to split, halo_cap + 1, on the last tile of a tiling
+    with a small halo_cap; more than PP_TILE_NODES_MAX nodes) is skipped by
+    the step's own bounds checks and reported as PP_STATUS_BAD_TILING;
+    write() raises."""
+    import probabilistic_peridynamics_gb300 as pp
+    from probabilistic_peridynamics_gb300 import _lib, tiling
+    from tests.gpu_helpers import breaking_setup
+    w = breaking_setup("velocity_verlet", 14, 12, 6)
+    integ = pp.VelocityVerletCUDA(0.5, 1.0, precision="mixed", tiled=True,
+                                  autotune=False)
+    n = w["nnodes"]
+    integ.build(n, 3, w["max_neigh"], w["coords"], w["volume"], w["family"],
+                w["bc_types"], w["bc_values"], w["force_bc_types"],
+                w["force_bc_values"], None, None, w.get("densities"))
+    z = np.zeros((n, 3))
+    if field == "split_mark":
+        monkeypatch.setattr(tiling, "HALO_CAP", 400)
+    integ.create_buffers(w["nlist"], w["n_neigh"], w["k"], w["s0"], None,
+                         z, z, z, z, z, np.zeros(n), None, 1, 1)
+    t = integ.tiling
+    if field == "halo_max":
+        t.halo_count_d[0] = _lib.PP_TILE_HALO_MAX + 1
+    elif field == "split_mark":
+        assert t.halo_cap == 400 < _lib.PP_TILE_HALO_MAX
+        t.halo_count_d[t.struct.ntiles - 1] = t.halo_cap + 1
+    else:
+        # the first tile's end moved past PP_TILE_NODES_MAX nodes
+        t.tile_start_d[1] = t.tile_start_d[0] + _lib.PP_TILE_NODES_MAX + 1
+    integ(0.0, 0.0)
+    zz = [np.zeros((n, 3)) for _ in range(5)]
+    with pytest.raises(_lib.LibraryError, match="device status 2"):
+        integ.write(*zz, np.zeros(n), w["nlist"].copy(), w["n_neigh"].copy())
