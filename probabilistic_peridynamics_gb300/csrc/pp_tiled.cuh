@@ -492,7 +492,10 @@ int launch_tiled_instance(const pp_fused_args& a, const pp_tiling& t, int parity
                           cudaStream_t st) {
     auto kernel = k_tiled<NW, CORR, TYPES, COMP, W, MINB>;
     // resident CTAs per SM: cached per kernel instance for the last
-    // dynamic shared-memory size (it varies with the table entries)
+    // dynamic shared-memory size (it varies with the table entries).  Two
+    // host threads racing here can only pair a size with another size's
+    // grid: a grid that does not fit at once still completes (the CTAs take
+    // tiles from the counter and never wait for one another).
     static size_t cached_dyn = 0;
     static int cached_grid = 0;
     const size_t dyn = dyn_smem(a);
